@@ -1,0 +1,334 @@
+#!/usr/bin/env python3
+"""Probe throughput of the GB300 hash-join engine on the 16M x 256M skewed join.
+
+Workload (default c2): 16M-row build side (INT32 keys Zipf(1.1) over 4M ranks,
+2 INT32 payloads with 20% NULLs, ASCII VARCHAR 8-64 B), 256M raw probe rows
+pre-filtered to ~25.6M by `pred < 100` (keys Zipf(1.1) over 8M ranks, 2 INT32
+payloads with 20% NULLs, VARCHAR), all payloads of both sides in the output.
+A step is one Contest::execute of that plan: page decode, unchained-table
+build, probe, and the output written as reference-format pages.
+
+  value  probe tuples/s with the input pages already resident in HBM
+         (device time of whole steps, CUDA events on the engine's stream)
+  e2e    the same through the C ABI with HOST input pages: upload, execute and
+         the copy of every result page back to host memory in the timed region
+  roofline  the probe phase (count + write kernels) against measured HBM
+         bandwidth, algorithmic bytes 4*N_probe + 8*D + 8*N_build + 8*N_out
+  cpu_baseline  the oracle restatement of the reference's execute() on a
+         bounded prefix of the probe side, all host threads
+
+The inputs (>2 GB of pages) exceed the 126 MB L2, so no flush is needed
+between steps.  `--impl reference` times the CPU restatement alone.
+Multi-GPU (torchrun): independent replicas, one per GPU (the path has no
+exchange step); value = all ranks' probe tuples / max step time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["c1", "c2", "c3"], default="c2")
+    ap.add_argument("--scale", type=float, default=1.0)
+    ap.add_argument("--cpu-sample", type=int, default=2_000_000,
+                    help="probe rows of the bounded CPU-baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------- distributed --
+
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ------------------------------------------------------------------ clocks --
+
+class Clocks:
+    """nvidia-smi samples (200 ms) of one GPU during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.p = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.p:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+
+    def summary(self) -> dict:
+        self.f.flush()
+        rows = []
+        for line in Path(self.f.name).read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(r[1]) for r in rows if num(r[1])]
+        mx = [num(r[2]) for r in rows if num(r[2])]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# --------------------------------------------------------------- workloads --
+
+def make_workload(hj, name: str, scale: float):
+    from hjgb300 import workloads
+    return getattr(workloads, name)(scale=scale)
+
+
+def peaks() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(workload: str):
+    """DRAM bytes per launch of the probe kernels from a committed ncu summary."""
+    p = ROOT / "profiles" / f"probe_traffic_{workload}.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text()).get("bytes_per_step")
+        except (ValueError, KeyError):
+            return None
+    return None
+
+
+def cpu_port_run(plan):
+    """Times one execute() of the oracle restatement; returns (seconds, rows)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    lib = oracle.port()
+    t = time.perf_counter()
+    out = oracle.run(lib, plan)
+    dt = time.perf_counter() - t
+    if out.status != 0:
+        raise RuntimeError(out.error)
+    return dt, out.num_rows
+
+
+# ------------------------------------------------------------------- ours ---
+
+def run_ours(args, d: Dist) -> dict:
+    import numpy as np
+    import torch
+    from __graft_entry__ import load
+
+    hj = load()
+    torch.cuda.set_device(d.local)
+    eng = hj.Engine(d.local)
+    eng.set_option("timing", 1)
+    w = make_workload(hj, args.workload, args.scale)
+    stream = torch.cuda.ExternalStream(eng.stream)
+
+    # ---- device-resident inputs
+    resident = hj.Plan(w.plan.nodes, [eng.upload(t) for t in w.plan.inputs], w.plan.root)
+    first = eng.execute_raw(resident)
+    nb, npr, nout, _ = eng.stats(first)
+    out_pages = []
+    L = hj.lib()
+    import ctypes as C
+    nrows, ncols = C.c_uint64(), C.c_uint32()
+    L.hj_result_shape(first, C.byref(nrows), C.byref(ncols))
+    for i in range(ncols.value):
+        ty, np_ = C.c_int32(), C.c_uint64()
+        L.hj_result_column(first, i, C.byref(ty), C.byref(np_))
+        out_pages.append(np_.value)
+    eng.free_result(first)
+    for _ in range(max(0, args.warmup - 1)):
+        eng.free_result(eng.execute_raw(resident))
+
+    phase_sum = {}
+    launches = 0
+    with Clocks(d.local) as clk:
+        d.barrier()
+        torch.cuda.synchronize()
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        start.record(stream)
+        for _ in range(args.steps):
+            r = eng.execute_raw(resident)
+            ph = eng.stats(r)[3]
+            for k, v in ph.items():
+                phase_sum[k] = phase_sum.get(k, 0.0) + v
+            launches += int(ph["launches"])
+            eng.free_result(r)
+        end.record(stream)
+        torch.cuda.synchronize()
+        d.barrier()
+    ms = d.max(start.elapsed_time(end) / args.steps)
+    clocks = clk.summary()
+    phases = {k: round(v / args.steps, 4) for k, v in phase_sum.items() if k != "launches"}
+
+    # ---- roofline of the probe phase
+    dir_bits = max(0, int(np.ceil(np.log2(max(1, nb)))))
+    D = (1 << dir_bits) + 1
+    a_probe = 4 * npr + 8 * D + 8 * nb + 8 * nout
+    t_probe = phases.get("probe", 0.0) / 1e3
+    peak, peak_kind = peaks()
+    achieved = a_probe / t_probe / 1e9 if t_probe > 0 else None
+    roofline = {"bound": "hbm", "kernel": "probe (k_probe_count + k_write_*)", "achieved": achieved,
+                "peak": peak, "unit": "GB/s", "frac": achieved / peak if achieved else None,
+                "traffic": ncu_traffic(args.workload), "algorithmic_bytes": a_probe,
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind}
+
+    # ---- end to end through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        host_bufs = [np.empty((n, hj.PAGE_SIZE), np.uint8) for n in out_pages]
+        h2d = sum(c.num_pages for t in w.plan.inputs for c in t.columns) * hj.PAGE_SIZE
+        d2h = sum(out_pages) * hj.PAGE_SIZE
+
+        def e2e_step():
+            r = eng.execute_raw(w.plan)
+            for i, buf in enumerate(host_bufs):
+                if buf.shape[0]:
+                    assert L.hj_result_copy_contiguous(eng.handle, r, i, buf.ctypes.data) == 0
+            eng.free_result(r)
+
+        e2e_step()
+        d.barrier()
+        torch.cuda.synchronize()
+        s2, e2 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        k2 = max(1, min(args.steps, 5))
+        s2.record(stream)
+        for _ in range(k2):
+            e2e_step()
+        e2.record(stream)
+        torch.cuda.synchronize()
+        ms2 = d.max(s2.elapsed_time(e2) / k2)
+        e2e = {"value": npr * d.world / (ms2 / 1e3), "unit": "probe tuples/s", "ms_per_step": ms2,
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+
+    # ---- CPU baseline (rank 0, bounded sample)
+    cpu = None
+    if d.rank == 0 and not args.no_cpu_baseline and w.sample is not None:
+        k = min(args.cpu_sample, w.probe_rows)
+        os.environ.setdefault("SIGMOD_THREADS", str(os.cpu_count() or 1))
+        dt, _ = cpu_port_run(w.sample(k))
+        cpu = {"value": k / dt, "unit": "probe tuples/s", "cores": int(os.environ["SIGMOD_THREADS"]),
+               "kind": "port",
+               "sample": f"first {k} of {w.probe_rows} probe rows against the full {w.build_rows}-row build "
+                         f"side, one execute() incl. build and output pages ({dt:.2f} s)"}
+
+    for t in resident.inputs:
+        eng.release(t)
+    eng.close()
+    return {
+        "metric": "probe tuples/s", "value": npr * d.world / (ms / 1e3), "unit": "tuples/s",
+        "n_gpus": d.world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic (seeded generator with the configured shapes; inputs > L2, no flush needed)",
+        "config": {"workload": f"{w.name}: {w.build_rows} build x {w.meta.get('probe_rows_raw', w.probe_rows)} "
+                               f"raw probe rows ({w.probe_rows} after the pre-filter)",
+                   "scale": args.scale, "build_tuples": nb, "probe_tuples": npr, "output_rows": nout,
+                   "parallelism": f"replicas x{d.world}", "l2": "inputs larger than L2"},
+        "phases_ms": phases, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+        "gpu_launches": launches, "clocks": clocks,
+    }
+
+
+def run_reference(args, d: Dist):
+    if d.rank != 0:
+        return None
+    from __graft_entry__ import load
+    hj = load()
+    w = make_workload(hj, args.workload, args.scale)
+    k = min(args.cpu_sample, w.probe_rows)
+    plan = w.sample(k) if w.sample else w.plan
+    threads = os.cpu_count() or 1
+    os.environ["SIGMOD_THREADS"] = str(threads)
+    for _ in range(args.warmup):
+        cpu_port_run(plan)
+    times = [cpu_port_run(plan)[0] for _ in range(args.steps)]
+    ms = 1e3 * sum(times) / len(times)
+    v = k / (ms / 1e3)
+    sample = (f"first {k} of {w.probe_rows} probe rows against the full {w.build_rows}-row build side; "
+              f"one execute() per step incl. build and output pages")
+    return {"impl": "reference", "metric": "probe tuples/s", "value": v, "unit": "tuples/s", "n_gpus": d.world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+            "config": {"workload": w.name, "scale": args.scale, "probe_tuples": k},
+            "cpu_baseline": {"value": v, "unit": "tuples/s", "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": "tuples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    args = parse()
+    d = Dist()
+    line = run_reference(args, d) if args.impl == "reference" else run_ours(args, d)
+    if d.rank == 0 and line is not None:
+        print(json.dumps(line), flush=True)
+    d.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,416 @@
+// Unchained hash-table build on the GPU.
+//
+// Semantics of UnchainedHash::finalize_build (include/unchained.h:155-217 of
+// the reference): Fibonacci hash, directory of 2^b words (default b =
+// log2(next_pow2(#tuples))), word = (first adjacency-array index << 16) |
+// 16-bit Bloom tag (OR of bloom_mask over the bucket's tuples), sentinel word
+// 2^b = #tuples << 16; the adjacency array holds the tuples grouped by bucket.
+// The directory words are therefore bit-identical to UnchainedHash's for the
+// same key multiset (only the order of tuples inside a bucket may differ).
+//
+// The reference's live table, PartitionedDirectoryHash
+// (include/partitioned_directory_hash.h:86-198), builds the same kind of
+// adjacency array on the host with per-thread slab buffers
+// (include/slab_allocator.h) and three phases.  Here the slabs are replaced by
+// a two-level MSD radix partition:
+//   1. k_part_hist      histogram of the top R hash bits (R = b - 13)
+//   2. k_part_offsets   partition offsets and per-partition chunk counts
+//   3. k_part_scatter   (key, row) pairs scattered to their partition
+//   4. k_bucket_count   per 8192-tuple chunk: shared-memory bucket counts and
+//                       Bloom tags over the partition's 2^13 buckets
+//   5. k_bucket_dir     per partition: prefix sum -> directory words
+//   6. k_bucket_scatter per chunk: tuples to their final adjacency slots
+//   7. k_bucket_mixed   flags buckets that hold more than one distinct key
+// Shared-memory histograms per chunk keep Zipf-heavy keys (one key can own
+// millions of tuples) off global atomics: a chunk adds one atomic per
+// non-empty bucket, and warp-aggregated shared atomics absorb duplicates.
+#include <algorithm>
+
+#include "hj_block.cuh"
+#include "hj_common.cuh"
+#include "hj_kernels.h"
+
+namespace hj {
+namespace {
+
+constexpr int kLocalBits   = 13;  // buckets per partition = 2^13 (64 KB of shared counters)
+constexpr int kMaxRadix    = 14;
+constexpr int kThreads     = 512;
+constexpr int kItems       = 16;
+constexpr int kTile        = kThreads * kItems;  // rows per partition-scatter tile
+constexpr int kChunk       = kTile;              // tuples per bucket chunk
+
+struct Geo {
+    uint32_t b;  // directory bits
+    uint32_t R;  // partition bits
+    uint32_t L;  // local bucket bits = b - R
+};
+
+__device__ __forceinline__ bool load_key(const KeyCol& kc, uint64_t i, int32_t& key) {
+    if (i >= kc.n) return false;
+    const uint64_t r = kc.rid ? uint64_t(__ldg(kc.rid + i)) : i;
+    if (!bit_valid(kc.valid, r)) return false;
+    key = __ldg(kc.vals + r);
+    return true;
+}
+
+// 1. Partition histogram + count of valid keys.
+__global__ void __launch_bounds__(kThreads)
+    k_part_hist(KeyCol kc, uint32_t R, uint32_t* __restrict__ part_cnt,
+                unsigned long long* __restrict__ n_valid) {
+    extern __shared__ uint32_t hist[];
+    const uint32_t P = 1u << R;
+    for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) hist[i] = 0;
+    __syncthreads();
+    uint32_t       mine   = 0;
+    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    for (uint64_t w0 = uint64_t(blockIdx.x) * blockDim.x + (threadIdx.x & ~31u); w0 < kc.n;
+         w0 += stride) {
+        int32_t        key;
+        const bool     ok  = load_key(kc, w0 + (threadIdx.x & 31), key);
+        const unsigned act = __ballot_sync(0xffffffffu, ok);
+        if (ok) {
+            const uint32_t part = uint32_t(bucket_of(fib_hash(key), R));
+            warp_agg_atomic_add(hist, part, act);
+            ++mine;
+        }
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < P; i += blockDim.x)
+        if (hist[i]) atomicAdd(part_cnt + i, hist[i]);
+    mine = warp_sum(mine);
+    if ((threadIdx.x & 31) == 0 && mine) atomicAdd(n_valid, (unsigned long long)mine);
+}
+
+// 2. Exclusive scans of partition sizes and chunk counts (one block).
+__global__ void __launch_bounds__(1024)
+    k_part_offsets(const uint32_t* __restrict__ part_cnt, uint32_t P, uint32_t* __restrict__ part_off,
+                   uint32_t* __restrict__ part_cursor, uint32_t* __restrict__ chunk_off) {
+    __shared__ uint32_t sm[33];
+    uint32_t            run_t = 0, run_c = 0;
+    for (uint32_t base = 0; base < P; base += blockDim.x) {
+        const uint32_t i  = base + threadIdx.x;
+        const uint32_t c  = i < P ? part_cnt[i] : 0;
+        const uint32_t ch = (c + kChunk - 1) / kChunk;
+        uint32_t       tot_t, tot_c;
+        const uint32_t et = block_exclusive_scan<uint32_t>(c, sm, &tot_t);
+        const uint32_t ec = block_exclusive_scan<uint32_t>(ch, sm, &tot_c);
+        if (i < P) {
+            part_off[i]    = run_t + et;
+            part_cursor[i] = run_t + et;
+            chunk_off[i]   = run_c + ec;
+        }
+        run_t += tot_t;
+        run_c += tot_c;
+    }
+    if (threadIdx.x == 0) {
+        part_off[P]  = run_t;
+        chunk_off[P] = run_c;
+    }
+}
+
+// 3. Scatter (key, row) to partitions.  Each block owns a tile of kTile rows:
+//    one global atomic per (tile, non-empty partition) reserves its space.
+__global__ void __launch_bounds__(kThreads)
+    k_part_scatter(KeyCol kc, uint32_t R, uint32_t* __restrict__ part_cursor,
+                   int32_t* __restrict__ tkey, uint32_t* __restrict__ trow) {
+    extern __shared__ uint32_t sh[];  // P counters, reused as bases
+    const uint32_t P     = 1u << R;
+    const uint64_t tile0 = uint64_t(blockIdx.x) * kTile;
+    for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) sh[i] = 0;
+    __syncthreads();
+    int32_t  keys[kItems];
+    uint32_t parts[kItems];
+    uint32_t okmask = 0;
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) {
+        const uint64_t i  = tile0 + uint64_t(k) * kThreads + threadIdx.x;
+        const bool     ok = load_key(kc, i, keys[k]);
+        parts[k]          = ok ? uint32_t(bucket_of(fib_hash(keys[k]), R)) : 0;
+        const unsigned act = __ballot_sync(0xffffffffu, ok);
+        if (ok) {
+            warp_agg_atomic_add(sh, parts[k], act);
+            okmask |= 1u << k;
+        }
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < P; i += blockDim.x)
+        if (sh[i]) sh[i] = atomicAdd(part_cursor + i, sh[i]);
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) {
+        const bool     ok  = (okmask >> k) & 1u;
+        const unsigned act = __ballot_sync(0xffffffffu, ok);
+        if (ok) {
+            const uint32_t pos = warp_agg_atomic_add(sh, parts[k], act);
+            tkey[pos]          = keys[k];
+            trow[pos]          = uint32_t(tile0 + uint64_t(k) * kThreads + threadIdx.x);
+        }
+    }
+}
+
+// Locates chunk `cid`: its partition and tuple range.  Returns false past the end.
+__device__ __forceinline__ bool chunk_range(uint32_t cid, const uint32_t* chunk_off,
+                                            const uint32_t* part_off, uint32_t P, uint32_t& part,
+                                            uint32_t& s, uint32_t& e, bool& single) {
+    if (cid >= chunk_off[P]) return false;
+    uint32_t lo = 0, hi = P;  // largest p with chunk_off[p] <= cid
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (chunk_off[mid] <= cid) lo = mid;
+        else                       hi = mid;
+    }
+    // skip empty partitions that share the same chunk_off
+    part             = lo;
+    const uint32_t k = cid - chunk_off[part];
+    s                = part_off[part] + k * kChunk;
+    e                = min(part_off[part + 1], s + kChunk);
+    single           = chunk_off[part + 1] - chunk_off[part] == 1;
+    return true;
+}
+
+// 4. Per-chunk bucket counts and Bloom tags.
+__global__ void __launch_bounds__(kThreads)
+    k_bucket_count(Geo g, const uint32_t* __restrict__ chunk_off, const uint32_t* __restrict__ part_off,
+                   const int32_t* __restrict__ tkey, uint32_t* __restrict__ gcnt,
+                   uint32_t* __restrict__ gbloom) {
+    extern __shared__ uint32_t sh[];
+    const uint32_t nl = 1u << g.L;
+    uint32_t*      cnt = sh;
+    uint32_t*      blm = sh + nl;
+    uint32_t       part, s, e;
+    bool           single;
+    if (!chunk_range(blockIdx.x, chunk_off, part_off, 1u << g.R, part, s, e, single)) return;
+    for (uint32_t i = threadIdx.x; i < 2 * nl; i += blockDim.x) sh[i] = 0;
+    __syncthreads();
+    const uint32_t lmask = nl - 1;
+    for (uint32_t w0 = s + (threadIdx.x & ~31u); w0 < e; w0 += blockDim.x) {
+        const uint32_t j  = w0 + (threadIdx.x & 31);
+        const bool     ok = j < e;
+        const unsigned act = __ballot_sync(0xffffffffu, ok);
+        if (ok) {
+            const uint64_t h     = fib_hash(tkey[j]);
+            const uint32_t local = uint32_t(bucket_of(h, g.b)) & lmask;
+            warp_agg_atomic_add(cnt, local, act);
+            warp_agg_atomic_or(blm, local, bloom_mask(h), act);
+        }
+    }
+    __syncthreads();
+    const uint64_t gb = uint64_t(part) << g.L;
+    for (uint32_t i = threadIdx.x; i < nl; i += blockDim.x) {
+        if (single) {
+            gcnt[gb + i]   = cnt[i];
+            gbloom[gb + i] = blm[i];
+        } else if (cnt[i]) {
+            atomicAdd(gcnt + gb + i, cnt[i]);
+            atomicOr(gbloom + gb + i, blm[i]);
+        }
+    }
+}
+
+// 5. Directory words.  One block per partition; gcnt becomes the scatter cursor.
+__global__ void __launch_bounds__(1024)
+    k_bucket_dir(Geo g, const uint32_t* __restrict__ part_off, uint32_t* __restrict__ gcnt,
+                 const uint32_t* __restrict__ gbloom, uint64_t* __restrict__ dir) {
+    __shared__ uint32_t sm[33];
+    const uint32_t part = blockIdx.x;
+    const uint32_t nl   = 1u << g.L;
+    const uint64_t gb   = uint64_t(part) << g.L;
+    const uint32_t P    = 1u << g.R;
+    uint32_t       run  = part_off[part];
+    if (part_off[part + 1] == run) {  // empty partition: all buckets empty
+        for (uint32_t i = threadIdx.x; i < nl; i += blockDim.x) {
+            dir[gb + i]  = uint64_t(run) << 16;
+            gcnt[gb + i] = run;
+        }
+    } else {
+        for (uint32_t base = 0; base < nl; base += blockDim.x) {
+            const uint32_t i = base + threadIdx.x;
+            const uint32_t c = i < nl ? gcnt[gb + i] : 0;
+            uint32_t       tot;
+            const uint32_t ex = block_exclusive_scan<uint32_t>(c, sm, &tot);
+            if (i < nl) {
+                const uint32_t start = run + ex;
+                dir[gb + i]          = (uint64_t(start) << 16) | (gbloom[gb + i] & 0xffffu);
+                gcnt[gb + i]         = start;
+            }
+            run += tot;
+        }
+    }
+    if (part == P - 1 && threadIdx.x == 0) dir[uint64_t(P) << g.L] = uint64_t(part_off[P]) << 16;
+}
+
+// 6. Final scatter into bucket order.
+__global__ void __launch_bounds__(kThreads)
+    k_bucket_scatter(Geo g, const uint32_t* __restrict__ chunk_off, const uint32_t* __restrict__ part_off,
+                     const int32_t* __restrict__ tkey, const uint32_t* __restrict__ trow,
+                     uint32_t* __restrict__ cursor, int32_t* __restrict__ okey,
+                     uint32_t* __restrict__ orow) {
+    extern __shared__ uint32_t sh[];
+    const uint32_t nl = 1u << g.L;
+    uint32_t       part, s, e;
+    bool           single;
+    if (!chunk_range(blockIdx.x, chunk_off, part_off, 1u << g.R, part, s, e, single)) return;
+    for (uint32_t i = threadIdx.x; i < nl; i += blockDim.x) sh[i] = 0;
+    __syncthreads();
+    const uint32_t lmask = nl - 1;
+    int32_t        keys[kItems];
+    uint32_t       loc[kItems];
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) {
+        const uint32_t j  = s + uint32_t(k) * kThreads + threadIdx.x;
+        const bool     ok = j < e;
+        keys[k]           = ok ? tkey[j] : 0;
+        loc[k]            = ok ? (uint32_t(bucket_of(fib_hash(keys[k]), g.b)) & lmask) : 0;
+        const unsigned act = __ballot_sync(0xffffffffu, ok);
+        if (ok) warp_agg_atomic_add(sh, loc[k], act);
+    }
+    __syncthreads();
+    const uint64_t gb = uint64_t(part) << g.L;
+    for (uint32_t i = threadIdx.x; i < nl; i += blockDim.x) {
+        if (sh[i]) sh[i] = single ? cursor[gb + i] : atomicAdd(cursor + gb + i, sh[i]);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) {
+        const uint32_t j   = s + uint32_t(k) * kThreads + threadIdx.x;
+        const bool     ok  = j < e;
+        const unsigned act = __ballot_sync(0xffffffffu, ok);
+        if (ok) {
+            const uint32_t pos = warp_agg_atomic_add(sh, loc[k], act);
+            okey[pos]          = keys[k];
+            orow[pos]          = trow[j];
+        }
+    }
+}
+
+// 7. mixed[p] bit set when bucket p holds two different keys.
+__global__ void k_bucket_mixed(uint32_t b, uint64_t n, const uint64_t* __restrict__ dir,
+                               const int32_t* __restrict__ key, uint32_t* __restrict__ mixed) {
+    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < n; j += stride) {
+        const int32_t  k     = key[j];
+        const uint64_t p     = bucket_of(fib_hash(k), b);
+        const uint64_t first = __ldg(dir + p) >> 16;
+        if (key[first] != k) atomicOr(mixed + (p >> 5), 1u << (p & 31));
+    }
+}
+
+uint32_t ceil_log2(uint64_t n) {
+    uint32_t b = 0;
+    while ((1ull << b) < n) ++b;
+    return b;
+}
+
+int grid_for(uint64_t work, int threads, int per_sm = 4) {
+    const uint64_t want = (work + threads - 1) / threads;
+    return int(std::min<uint64_t>(std::max<uint64_t>(want, 1), uint64_t(kSMs) * per_sm));
+}
+
+}  // namespace
+
+void build_table(const KeyCol& kc, int dir_bits, int radix_bits, Table& t, uint64_t* scratch_host,
+                 cudaStream_t st) {
+    t = Table{};
+    const uint32_t b_upper = dir_bits >= 0 ? uint32_t(dir_bits) : ceil_log2(std::max<uint64_t>(kc.n, 1));
+    uint32_t       R       = radix_bits >= 0 ? uint32_t(radix_bits)
+                                             : (b_upper > kLocalBits ? b_upper - kLocalBits : 0);
+    if (R > kMaxRadix) throw Error(HJ_ERR_INVALID, "build side too large for the radix partition");
+
+    unsigned long long* d_nvalid = dalloc_n<unsigned long long>(1, st);
+    uint32_t*           part_cnt = nullptr;
+    auto run_hist = [&](uint32_t r) {
+        const uint32_t P = 1u << r;
+        part_cnt         = dalloc_n<uint32_t>(P, st);
+        HJ_CUDA(cudaMemsetAsync(part_cnt, 0, P * sizeof(uint32_t), st));
+        HJ_CUDA(cudaMemsetAsync(d_nvalid, 0, sizeof(unsigned long long), st));
+        const size_t smem = P * sizeof(uint32_t);
+        if (smem > 48 * 1024)
+            HJ_CUDA(cudaFuncSetAttribute(k_part_hist, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         int(smem)));
+        k_part_hist<<<grid_for(kc.n, kThreads), kThreads, smem, st>>>(kc, r, part_cnt, d_nvalid);
+        HJ_LAUNCH_CHECK();
+        HJ_CUDA(cudaMemcpyAsync(scratch_host, d_nvalid, sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+        HJ_CUDA(cudaStreamSynchronize(st));
+    };
+    run_hist(R);
+    const uint64_t nv = scratch_host[0];
+    if (nv == 0) {  // UnchainedHash with no tuples: no directory, every probe misses
+        dfree(part_cnt, st);
+        dfree(d_nvalid, st);
+        return;
+    }
+    if (nv > 0xffffffffull) throw Error(HJ_ERR_INVALID, "more than 2^32 build tuples");
+    const uint32_t b = dir_bits >= 0 ? uint32_t(dir_bits) : ceil_log2(nv);
+    if (R > b) {  // NULLs shrank the directory below the partition fan-out
+        dfree(part_cnt, st);
+        R = b;
+        run_hist(R);
+    }
+    if (b - R > kLocalBits) throw Error(HJ_ERR_INVALID, "radix_bits too small for the directory");
+    const Geo      g{b, R, b - R};
+    const uint32_t P = 1u << R;
+
+    uint32_t* part_off    = dalloc_n<uint32_t>(P + 1, st);
+    uint32_t* part_cursor = dalloc_n<uint32_t>(P, st);
+    uint32_t* chunk_off   = dalloc_n<uint32_t>(P + 1, st);
+    k_part_offsets<<<1, 1024, 0, st>>>(part_cnt, P, part_off, part_cursor, chunk_off);
+    HJ_LAUNCH_CHECK();
+
+    int32_t*  tkey = dalloc_n<int32_t>(nv, st);
+    uint32_t* trow = dalloc_n<uint32_t>(nv, st);
+    {
+        const size_t smem = P * sizeof(uint32_t);
+        if (smem > 48 * 1024)
+            HJ_CUDA(cudaFuncSetAttribute(k_part_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         int(smem)));
+        k_part_scatter<<<div_up(kc.n, kTile), kThreads, smem, st>>>(kc, R, part_cursor, tkey, trow);
+        HJ_LAUNCH_CHECK();
+    }
+
+    const uint64_t nb     = 1ull << b;
+    t.dir_bits            = b;
+    t.n_tuples            = nv;
+    t.dir                 = dalloc_n<uint64_t>(nb + 1, st);
+    t.keys                = dalloc_n<int32_t>(nv, st);
+    t.rows                = dalloc_n<uint32_t>(nv, st);
+    t.mixed               = dalloc_n<uint32_t>((nb + 31) / 32, st);
+    uint32_t* gcnt        = dalloc_n<uint32_t>(nb, st);
+    uint32_t* gbloom      = dalloc_n<uint32_t>(nb, st);
+    HJ_CUDA(cudaMemsetAsync(gcnt, 0, nb * sizeof(uint32_t), st));
+    HJ_CUDA(cudaMemsetAsync(gbloom, 0, nb * sizeof(uint32_t), st));
+    HJ_CUDA(cudaMemsetAsync(t.mixed, 0, ((nb + 31) / 32) * sizeof(uint32_t), st));
+
+    const unsigned chunks_upper = unsigned((nv + kChunk - 1) / kChunk + P);
+    {
+        const size_t smem = 2 * (size_t(1) << g.L) * sizeof(uint32_t);
+        HJ_CUDA(cudaFuncSetAttribute(k_bucket_count, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     int(smem)));
+        k_bucket_count<<<chunks_upper, kThreads, smem, st>>>(g, chunk_off, part_off, tkey, gcnt, gbloom);
+        HJ_LAUNCH_CHECK();
+    }
+    k_bucket_dir<<<P, 1024, 0, st>>>(g, part_off, gcnt, gbloom, t.dir);
+    HJ_LAUNCH_CHECK();
+    {
+        const size_t smem = (size_t(1) << g.L) * sizeof(uint32_t);
+        HJ_CUDA(cudaFuncSetAttribute(k_bucket_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     int(smem)));
+        k_bucket_scatter<<<chunks_upper, kThreads, smem, st>>>(g, chunk_off, part_off, tkey, trow, gcnt,
+                                                              t.keys, t.rows);
+        HJ_LAUNCH_CHECK();
+    }
+    k_bucket_mixed<<<grid_for(nv, 256, 8), 256, 0, st>>>(b, nv, t.dir, t.keys, t.mixed);
+    HJ_LAUNCH_CHECK();
+
+    for (void* p : {(void*)d_nvalid, (void*)part_cnt, (void*)part_off, (void*)part_cursor,
+                    (void*)chunk_off, (void*)tkey, (void*)trow, (void*)gcnt, (void*)gbloom})
+        dfree(p, st);
+}
+
+void free_table(Table& t, cudaStream_t st) {
+    for (void* p : {(void*)t.dir, (void*)t.keys, (void*)t.rows, (void*)t.mixed})
+        if (p) dfree(p, st);
+    t = Table{};
+}
+
+}  // namespace hj

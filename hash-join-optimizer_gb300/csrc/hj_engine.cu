@@ -1,0 +1,929 @@
+// Host runtime of the GB300 join engine and its C ABI (include/hj_api.h).
+//
+// Device form of Contest::execute (src/execute.cpp:584-608 of the reference):
+//   * inputs: each (table, column) a scan touches is uploaded once per call
+//     (or found resident in HBM) as its raw 8 KiB pages, then decoded on the
+//     GPU (copy_scan, execute.cpp:265-369);
+//   * intermediates: a join result is a set of row-id vectors, one per base
+//     table instance ("source") that its output columns still reference, plus
+//     the (source, input column) of every output column.  This is the device
+//     column_t (include/column_t.h): a column_t in "direct" mode over an input
+//     column, seen through a selection vector.  Values stay in the input
+//     columns; only 4-byte row ids move between joins;
+//   * joins: build the unchained table on the build side's key, probe with the
+//     probe side's key, write one composed row-id vector per needed source
+//     (JoinAlgorithm::run, execute.cpp:26-186);
+//   * output: the root's columns are written as pages in HBM
+//     (table_to_columnar, execute.cpp:431-573), VARCHAR bytes gathered through
+//     their StrRef only there.
+#include <algorithm>
+#include <atomic>
+#include <condition_variable>
+#include <cstdio>
+#include <cstring>
+#include <functional>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/hj_api.h"
+#include "../../include/value_t.h"
+#include "hj_common.cuh"
+#include "hj_kernels.h"
+
+namespace hj {
+
+std::atomic<uint64_t> g_kernel_launches{0};
+
+// ---------------------------------------------------------------- memory ----
+
+void* dalloc(size_t bytes, cudaStream_t st) {
+    void* p = nullptr;
+    if (bytes == 0) bytes = 16;
+    const cudaError_t e = cudaMallocAsync(&p, bytes, st);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        throw Error(HJ_ERR_NOMEM, "device allocation of " + std::to_string(bytes) + " bytes failed: "
+                                      + cudaGetErrorString(e));
+    }
+    return p;
+}
+
+void dfree(void* p, cudaStream_t st) {
+    if (p) cudaFreeAsync(p, st);
+}
+
+namespace {
+
+// Device buffer freed (stream-ordered) when the last reference goes.
+struct DevBuf {
+    void*        p  = nullptr;
+    cudaStream_t st = nullptr;
+    DevBuf(size_t bytes, cudaStream_t s) : p(dalloc(bytes, s)), st(s) {}
+    DevBuf(void* adopt, cudaStream_t s) : p(adopt), st(s) {}
+    ~DevBuf() { dfree(p, st); }
+    template <class T>
+    T* as() const { return static_cast<T*>(p); }
+};
+using Buf = std::shared_ptr<DevBuf>;
+
+Buf make_buf(size_t bytes, cudaStream_t st) { return std::make_shared<DevBuf>(bytes, st); }
+
+// ------------------------------------------------------------ host threads --
+
+class ThreadPool {
+public:
+    explicit ThreadPool(unsigned n) {
+        for (unsigned i = 0; i < n; ++i) workers_.emplace_back([this] { loop(); });
+    }
+    ~ThreadPool() {
+        {
+            std::lock_guard<std::mutex> g(mu_);
+            stop_ = true;
+        }
+        cv_.notify_all();
+        for (auto& w : workers_) w.join();
+    }
+    unsigned size() const { return unsigned(workers_.size()); }
+
+    // Runs fn(i) for i in [0, n) on the pool and the calling thread.
+    void parallel_for(size_t n, const std::function<void(size_t)>& fn) {
+        if (n == 0) return;
+        if (n == 1 || workers_.empty()) {
+            for (size_t i = 0; i < n; ++i) fn(i);
+            return;
+        }
+        std::atomic<size_t> next{0};
+        std::atomic<size_t> done{0};
+        const size_t        helpers = std::min<size_t>(workers_.size(), n - 1);
+        auto body = [&] {
+            for (size_t i; (i = next.fetch_add(1)) < n;) fn(i);
+        };
+        {
+            std::lock_guard<std::mutex> g(mu_);
+            for (size_t h = 0; h < helpers; ++h)
+                jobs_.push_back([&] {
+                    body();
+                    done.fetch_add(1);
+                });
+        }
+        cv_.notify_all();
+        body();
+        while (done.load() < helpers) std::this_thread::yield();
+    }
+
+private:
+    void loop() {
+        for (;;) {
+            std::function<void()> job;
+            {
+                std::unique_lock<std::mutex> lk(mu_);
+                cv_.wait(lk, [this] { return stop_ || !jobs_.empty(); });
+                if (stop_ && jobs_.empty()) return;
+                job = std::move(jobs_.back());
+                jobs_.pop_back();
+            }
+            job();
+        }
+    }
+    std::vector<std::thread>           workers_;
+    std::vector<std::function<void()>> jobs_;
+    std::mutex                         mu_;
+    std::condition_variable            cv_;
+    bool                               stop_ = false;
+};
+
+// ------------------------------------------------------------ input tables --
+
+struct DevColumn {
+    int32_t  type      = HJ_INT32;
+    uint64_t num_pages = 0;
+    Buf      pages;  // raw pages, contiguous
+    // decoded form (per execute call)
+    uint64_t rows     = 0;
+    uint64_t non_null = 0;
+    Buf      vals;   // INT32 values
+    Buf      valid;  // validity bitmap (nullptr: no NULLs)
+    Buf      refs;   // VARCHAR value_t
+    bool     decoded  = false;
+    bool     page_overflow = false;  // a page index > 2^18-1 carries strings
+};
+
+struct DevTable {
+    uint64_t               num_rows = 0;
+    std::vector<DevColumn> cols;
+};
+
+}  // namespace
+}  // namespace hj
+
+// ------------------------------------------------------------------ context --
+
+struct hj_context {
+    int                 device = 0;
+    cudaStream_t        st     = nullptr;
+    std::string         err;
+    int64_t             dir_bits    = -1;
+    int64_t             radix_bits  = -1;
+    int64_t             probe_group = 8;
+    int64_t             light_max   = 32;
+    int64_t             timing      = 0;
+    uint64_t*           pinned      = nullptr;  // small readbacks
+    uint8_t*            staging     = nullptr;  // pinned transfer ring
+    size_t              staging_bytes = 0;
+    cudaEvent_t         slot_ev[2]  = {nullptr, nullptr};
+    std::unique_ptr<hj::ThreadPool>         pool;
+    std::map<uint64_t, std::shared_ptr<hj::DevTable>> resident;
+    uint64_t            next_handle = 1;
+};
+
+struct hj_result {
+    uint64_t num_rows = 0;
+    struct Col {
+        int32_t  type;
+        uint64_t num_pages;
+        hj::Buf  pages;
+    };
+    std::vector<Col> cols;
+    uint64_t         build_tuples = 0, probe_tuples = 0, output_rows = 0;
+    uint64_t         kernel_launches = 0;     // kernels this execute launched
+    std::map<std::string, double> phase_ms;  // filled when option "timing" is 1
+};
+
+struct hj_hash_table {
+    hj::Table    t;
+    cudaStream_t st;
+};
+
+namespace hj {
+namespace {
+
+thread_local std::string g_create_error;
+
+constexpr size_t kSlot = 64ull << 20;  // pinned staging slot (two slots)
+
+void ensure_staging(hj_context* c) {
+    if (c->staging) return;
+    c->staging_bytes = 2 * kSlot;
+    HJ_CUDA(cudaMallocHost(&c->staging, c->staging_bytes));
+    for (auto& e : c->slot_ev) HJ_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+}
+
+// Copies `n` host pages into the contiguous device buffer `dst`: pages are
+// gathered by the host threads into a pinned slot while the previous slot is
+// in flight.
+void upload_pages(hj_context* c, const void* const* pages, uint64_t n, uint8_t* dst) {
+    if (n == 0) return;
+    ensure_staging(c);
+    const uint64_t per_slot = kSlot / kPage;
+    int            slot     = 0;
+    for (uint64_t p0 = 0; p0 < n; p0 += per_slot, slot ^= 1) {
+        const uint64_t cnt = std::min(per_slot, n - p0);
+        uint8_t*       buf = c->staging + size_t(slot) * kSlot;
+        HJ_CUDA(cudaEventSynchronize(c->slot_ev[slot]));
+        const uint64_t per_task = 256;
+        c->pool->parallel_for((cnt + per_task - 1) / per_task, [&](size_t t) {
+            const uint64_t a = t * per_task, b = std::min(cnt, a + per_task);
+            for (uint64_t i = a; i < b; ++i) std::memcpy(buf + i * kPage, pages[p0 + i], kPage);
+        });
+        HJ_CUDA(cudaMemcpyAsync(dst + p0 * kPage, buf, cnt * kPage, cudaMemcpyHostToDevice, c->st));
+        HJ_CUDA(cudaEventRecord(c->slot_ev[slot], c->st));
+    }
+}
+
+// Copies `n` device pages to host pages dst[i] (or one contiguous buffer).
+void download_pages(hj_context* c, const uint8_t* src, uint64_t n, void* const* dst, uint8_t* contig) {
+    if (n == 0) return;
+    ensure_staging(c);
+    const uint64_t per_slot = kSlot / kPage;
+    int            slot     = 0;
+    uint64_t       pend_p0 = 0, pend_cnt = 0;
+    int            pend_slot = -1;
+    auto drain = [&]() {
+        if (pend_slot < 0) return;
+        HJ_CUDA(cudaEventSynchronize(c->slot_ev[pend_slot]));
+        uint8_t*       buf      = c->staging + size_t(pend_slot) * kSlot;
+        const uint64_t per_task = 256;
+        c->pool->parallel_for((pend_cnt + per_task - 1) / per_task, [&](size_t t) {
+            const uint64_t a = t * per_task, b = std::min(pend_cnt, a + per_task);
+            if (contig) {
+                std::memcpy(contig + (pend_p0 + a) * kPage, buf + a * kPage, (b - a) * kPage);
+            } else {
+                for (uint64_t i = a; i < b; ++i) std::memcpy(dst[pend_p0 + i], buf + i * kPage, kPage);
+            }
+        });
+        pend_slot = -1;
+    };
+    for (uint64_t p0 = 0; p0 < n; p0 += per_slot, slot ^= 1) {
+        const uint64_t cnt = std::min(per_slot, n - p0);
+        uint8_t*       buf = c->staging + size_t(slot) * kSlot;
+        HJ_CUDA(cudaMemcpyAsync(buf, src + p0 * kPage, cnt * kPage, cudaMemcpyDeviceToHost, c->st));
+        HJ_CUDA(cudaEventRecord(c->slot_ev[slot], c->st));
+        drain();  // copy out the previous slot while this one transfers
+        pend_p0   = p0;
+        pend_cnt  = cnt;
+        pend_slot = slot;
+    }
+    drain();
+}
+
+// Uploads the listed columns of a host table (others stay empty).
+std::shared_ptr<DevTable> upload_table(hj_context* c, const hj_table_desc& t,
+                                       const std::vector<bool>& want) {
+    auto dt      = std::make_shared<DevTable>();
+    dt->num_rows = t.num_rows;
+    dt->cols.resize(t.num_columns);
+    for (uint32_t i = 0; i < t.num_columns; ++i) {
+        DevColumn& d = dt->cols[i];
+        d.type       = t.columns[i].type;
+        d.num_pages  = t.columns[i].num_pages;
+        if (!want.empty() && !want[i]) continue;
+        d.pages = make_buf(std::max<uint64_t>(d.num_pages, 1) * kPage, c->st);
+        upload_pages(c, t.columns[i].pages, d.num_pages, d.pages->as<uint8_t>());
+    }
+    return dt;
+}
+
+// Decodes a device column (idempotent within one execute call).
+void decode_column(hj_context* c, DevColumn& d, uint32_t table_id, uint32_t col_idx) {
+    if (d.decoded) return;
+    d.decoded = true;
+    d.rows = d.non_null = 0;
+    if (d.type != HJ_INT32 && d.type != HJ_VARCHAR) return;  // the reference skips these types
+    if (d.num_pages == 0) return;
+    if (!d.pages) throw Error(HJ_ERR_INVALID, "column pages were not uploaded");
+    cudaStream_t st  = c->st;
+    const uint64_t np = d.num_pages;
+    uint32_t* rows  = dalloc_n<uint32_t>(np, st);
+    uint32_t* nn    = dalloc_n<uint32_t>(np, st);
+    uint32_t* flags = dalloc_n<uint32_t>(np, st);
+    uint64_t* rs    = dalloc_n<uint64_t>(np + 1, st);
+    uint64_t* nns   = dalloc_n<uint64_t>(np + 1, st);
+    uint64_t* fl    = dalloc_n<uint64_t>(np + 1, st);
+    launch_page_headers(d.pages->as<uint8_t>(), np, d.type, rows, nn, flags, st);
+    scan_exclusive_u32_to_u64(rows, rs, np, st);
+    scan_exclusive_u32_to_u64(nn, nns, np, st);
+    // flags: count pages with NULLs (bit 0) and with overflowing StrRef pages (bit 1)
+    // by scanning them as integers: bit 1 pages add 2^32.
+    HJ_CUDA(cudaMemcpyAsync(c->pinned, rs + np, 8, cudaMemcpyDeviceToHost, st));
+    HJ_CUDA(cudaMemcpyAsync(c->pinned + 1, nns + np, 8, cudaMemcpyDeviceToHost, st));
+    HJ_CUDA(cudaStreamSynchronize(st));
+    d.rows     = c->pinned[0];
+    d.non_null = c->pinned[1];
+    if (d.type == HJ_VARCHAR && np > StrRef::PAGE_MASK + 1) {
+        // any string on a page beyond the 18-bit page field overflows StrRef
+        std::vector<uint32_t> hf(np);
+        HJ_CUDA(cudaMemcpyAsync(hf.data(), flags, np * 4, cudaMemcpyDeviceToHost, st));
+        HJ_CUDA(cudaStreamSynchronize(st));
+        for (uint64_t p = StrRef::PAGE_MASK + 1; p < np; ++p)
+            if (hf[p] & 2u) {
+                for (void* q : {(void*)rows, (void*)nn, (void*)flags, (void*)rs, (void*)nns, (void*)fl})
+                    dfree(q, st);
+                throw Error(HJ_ERR_OUT_OF_RANGE, "StrRef page overflow: " + std::to_string(p) + " > "
+                                                     + std::to_string(StrRef::PAGE_MASK));
+            }
+    }
+    if (d.type == HJ_VARCHAR && d.non_null > 0) {
+        if (table_id > StrRef::TABLE_MASK)
+            throw Error(HJ_ERR_OUT_OF_RANGE, "StrRef table overflow: " + std::to_string(table_id)
+                                                 + " > " + std::to_string(StrRef::TABLE_MASK));
+        if (col_idx > StrRef::COLUMN_MASK)
+            throw Error(HJ_ERR_OUT_OF_RANGE, "StrRef column overflow: " + std::to_string(col_idx)
+                                                 + " > " + std::to_string(StrRef::COLUMN_MASK));
+    }
+    const uint64_t words = (d.rows + 31) / 32 + 1;
+    if (d.type == HJ_INT32) {
+        d.vals = make_buf(std::max<uint64_t>(d.rows, 1) * 4, st);
+        if (d.non_null != d.rows) {
+            d.valid = make_buf(words * 4, st);
+            HJ_CUDA(cudaMemsetAsync(d.valid->p, 0, words * 4, st));
+        }
+        launch_decode_int32(d.pages->as<uint8_t>(), np, rs, d.vals->as<int32_t>(),
+                            d.valid ? d.valid->as<uint32_t>() : nullptr, st);
+    } else {
+        d.refs  = make_buf(std::max<uint64_t>(d.rows, 1) * 8, st);
+        d.valid = make_buf(words * 4, st);
+        HJ_CUDA(cudaMemsetAsync(d.valid->p, 0, words * 4, st));
+        launch_decode_varchar(d.pages->as<uint8_t>(), np, rs, table_id, col_idx, d.refs->as<uint64_t>(),
+                              d.valid->as<uint32_t>(), st);
+    }
+    for (void* q : {(void*)rows, (void*)nn, (void*)flags, (void*)rs, (void*)nns, (void*)fl}) dfree(q, st);
+}
+
+// ------------------------------------------------------------ intermediates --
+
+struct Source {
+    uint32_t table;  // input table id
+    Buf      rid;    // row ids into the input table's columns; null = identity
+};
+
+struct ColRef {
+    int      src;    // index into Inter::srcs
+    uint32_t table;
+    uint32_t col;
+};
+
+struct Inter {
+    uint64_t               rows = 0;
+    std::vector<Source>    srcs;
+    std::vector<ColRef>    cols;
+};
+
+struct Exec {
+    hj_context*                            c;
+    const hj_plan_desc&                    plan;
+    std::vector<std::shared_ptr<DevTable>> tables;
+    uint64_t                               build_tuples = 0, probe_tuples = 0, out_rows = 0;
+    std::vector<std::pair<std::string, cudaEvent_t>> marks;  // phase boundaries (timing)
+
+    // Starts phase `name` on the stream (no-op unless option "timing" is set).
+    void phase(const char* name) {
+        if (!c->timing) return;
+        cudaEvent_t e;
+        HJ_CUDA(cudaEventCreate(&e));
+        HJ_CUDA(cudaEventRecord(e, c->st));
+        marks.emplace_back(name, e);
+    }
+
+    // Closes the last phase and sums device time per phase name (after sync).
+    void collect(std::map<std::string, double>& out) {
+        if (marks.empty()) return;
+        phase("");
+        HJ_CUDA(cudaEventSynchronize(marks.back().second));
+        for (size_t i = 0; i + 1 < marks.size(); ++i) {
+            float ms = 0;
+            HJ_CUDA(cudaEventElapsedTime(&ms, marks[i].second, marks[i + 1].second));
+            out[marks[i].first] += ms;
+        }
+        float tot = 0;
+        HJ_CUDA(cudaEventElapsedTime(&tot, marks.front().second, marks.back().second));
+        out["total"] = tot;
+    }
+
+    ~Exec() {
+        for (auto& m : marks) cudaEventDestroy(m.second);
+    }
+
+    DevColumn& column(uint32_t t, uint32_t col) {
+        DevColumn& d = tables[t]->cols[col];
+        decode_column(c, d, t, col);
+        return d;
+    }
+
+    Inter scan(const hj_node_desc& n) {
+        Inter in;
+        const uint32_t t = uint32_t(n.base_table_id);
+        in.srcs.push_back(Source{t, nullptr});
+        for (uint32_t a = 0; a < n.num_attrs; ++a) {
+            const uint32_t col = uint32_t(n.attrs[a].index);
+            in.cols.push_back(ColRef{0, t, col});
+        }
+        // rows: those of the first output column, as the reference's result
+        // columns count them (column_t::rows_num)
+        if (n.num_attrs > 0) in.rows = column(t, uint32_t(n.attrs[0].index)).rows;
+        return in;
+    }
+
+    // Number of non-NULL rows of a column seen through a source's row ids.
+    uint64_t non_null_through(const Inter& in, const ColRef& cr) {
+        DevColumn& d = column(cr.table, cr.col);
+        if (!in.srcs[cr.src].rid) return d.non_null;
+        if (d.non_null == 0 || in.rows == 0) return 0;
+        if (d.non_null == d.rows && !d.valid) return in.rows;
+        // count through the row ids on the host (rare path: VARCHAR join keys)
+        std::vector<uint32_t> rid(in.rows), bm((d.rows + 31) / 32 + 1);
+        HJ_CUDA(cudaMemcpyAsync(rid.data(), in.srcs[cr.src].rid->p, in.rows * 4, cudaMemcpyDeviceToHost, c->st));
+        HJ_CUDA(cudaMemcpyAsync(bm.data(), d.valid->p, bm.size() * 4, cudaMemcpyDeviceToHost, c->st));
+        HJ_CUDA(cudaStreamSynchronize(c->st));
+        uint64_t k = 0;
+        for (uint32_t r : rid) k += (bm[r >> 5] >> (r & 31)) & 1u;
+        return k;
+    }
+
+    KeyCol key_col(const Inter& in, const ColRef& cr) {
+        DevColumn& d = column(cr.table, cr.col);
+        KeyCol     k{};
+        k.n = in.rows;
+        if (d.type != HJ_INT32) {  // INT64/FP64 key: the reference's key column is empty
+            k.n = 0;
+            return k;
+        }
+        if (d.rows == 0) k.n = 0;
+        k.vals  = d.vals ? d.vals->as<int32_t>() : nullptr;
+        k.valid = d.valid ? d.valid->as<uint32_t>() : nullptr;
+        k.rid   = in.srcs[cr.src].rid ? in.srcs[cr.src].rid->as<uint32_t>() : nullptr;
+        return k;
+    }
+
+    Inter join(const hj_node_desc& n) {
+        Inter left  = run(n.left);
+        Inter right = run(n.right);
+        const bool bl = n.build_left != 0;
+        Inter& B = bl ? left : right;
+        Inter& P = bl ? right : left;
+        const uint64_t battr = bl ? n.left_attr : n.right_attr;
+        const uint64_t pattr = bl ? n.right_attr : n.left_attr;
+        if (battr >= B.cols.size() || pattr >= P.cols.size())
+            throw Error(HJ_ERR_INVALID, "join attribute out of range");
+        const ColRef bk = B.cols[battr], pk = P.cols[pattr];
+        // Non-INT32 join keys: the reference throws on the first non-NULL value
+        // (execute.cpp:81,130).
+        for (auto [in, cr] : {std::pair<Inter*, ColRef>{&B, bk}, std::pair<Inter*, ColRef>{&P, pk}}) {
+            DevColumn& d = column(cr.table, cr.col);
+            if (d.type == HJ_VARCHAR && non_null_through(*in, cr) > 0)
+                throw Error(HJ_ERR_RUNTIME, "Join key isn't of type int32_t");
+        }
+        // Output columns: left ++ right (execute.cpp:140-152)
+        Inter out;
+        std::vector<std::pair<int, int>> need;  // (side 0 probe / 1 build, source index)
+        auto src_slot = [&](int side, int s) {
+            for (size_t i = 0; i < need.size(); ++i)
+                if (need[i] == std::make_pair(side, s)) return int(i);
+            need.emplace_back(side, s);
+            return int(need.size() - 1);
+        };
+        for (uint32_t a = 0; a < n.num_attrs; ++a) {
+            const uint64_t idx = n.attrs[a].index;
+            const bool     from_left = idx < left.cols.size();
+            if (!from_left && idx - left.cols.size() >= right.cols.size())
+                throw Error(HJ_ERR_INVALID, "output attribute out of range");
+            const ColRef cr   = from_left ? left.cols[idx] : right.cols[idx - left.cols.size()];
+            const bool   is_b = from_left == bl;
+            out.cols.push_back(ColRef{src_slot(is_b ? 1 : 0, cr.src), cr.table, cr.col});
+        }
+        KeyCol bkc = key_col(B, bk), pkc = key_col(P, pk);
+        build_tuples += bkc.n;
+        probe_tuples += pkc.n;
+        Table t;
+        phase("build");
+        build_table(bkc, int(c->dir_bits), int(c->radix_bits), t, c->pinned, c->st);
+        phase("probe");
+        ProbeParams prm;
+        prm.light_max = int(c->light_max);
+        prm.group     = int(c->probe_group);
+        prm.pinned    = c->pinned;
+        ProbePlan* pp = nullptr;
+        uint64_t total = 0;
+        try {
+            total = probe_count(t, pkc, prm, &pp, c->st);
+            if (total > 0xffffffffull) throw Error(HJ_ERR_INVALID, "join result exceeds 2^32 rows");
+            out.rows = total;
+            std::vector<RidOut> ro;
+            for (auto [side, s] : need) {
+                Inter& side_in = side == 1 ? B : P;
+                Buf    dst     = make_buf(std::max<uint64_t>(total, 1) * 4, c->st);
+                ro.push_back(RidOut{side, side_in.srcs[s].rid ? side_in.srcs[s].rid->as<uint32_t>() : nullptr,
+                                    dst->as<uint32_t>()});
+                out.srcs.push_back(Source{side_in.srcs[s].table, dst});
+            }
+            if (total > 0) probe_write(t, pkc, pp, ro.data(), int(ro.size()), c->st);
+        } catch (...) {
+            probe_free(pp, c->st);
+            free_table(t, c->st);
+            throw;
+        }
+        probe_free(pp, c->st);
+        free_table(t, c->st);
+        out_rows += total;
+        return out;
+    }
+
+    Inter run(uint64_t node) {
+        if (node >= plan.num_nodes) throw Error(HJ_ERR_INVALID, "plan node out of range");
+        const hj_node_desc& n = plan.nodes[node];
+        if (n.kind == HJ_NODE_SCAN) {
+            if (n.base_table_id >= plan.num_inputs) throw Error(HJ_ERR_INVALID, "scan table out of range");
+            return scan(n);
+        }
+        if (n.kind != HJ_NODE_JOIN) throw Error(HJ_ERR_INVALID, "unknown node kind");
+        return join(n);
+    }
+
+    void materialize(const Inter& in, const hj_node_desc& root, hj_result* res) {
+        phase("materialize");
+        for (uint32_t a = 0; a < root.num_attrs; ++a) {
+            const ColRef&   cr = in.cols[a];
+            const int32_t   ty = root.attrs[a].type;
+            DevColumn&      d  = column(cr.table, cr.col);
+            const uint32_t* rid = in.srcs[cr.src].rid ? in.srcs[cr.src].rid->as<uint32_t>() : nullptr;
+            hj_result::Col  oc{ty, 0, nullptr};
+            // rows of this output column: the scan column's own count at a scan root
+            const uint64_t rows = in.srcs[cr.src].rid ? in.rows : d.rows;
+            if (ty == HJ_INT32) {
+                // A StrRef in an INT32 output column leaves the reference's bitmap
+                // undefined (execute.cpp:467-485); it is rejected here.
+                if (d.type == HJ_VARCHAR && non_null_through(in, cr) > 0)
+                    throw Error(HJ_ERR_RUNTIME, "VARCHAR value in an INT32 output column");
+                if ((d.type == HJ_INT32 || d.type == HJ_VARCHAR) && rows > 0) {
+                    oc.num_pages = (rows + kDenseRows - 1) / kDenseRows;
+                    oc.pages     = make_buf(oc.num_pages * kPage, c->st);
+                    launch_write_int32_pages(d.vals ? d.vals->as<int32_t>() : nullptr,
+                                             d.valid ? d.valid->as<uint32_t>() : nullptr, rid, rows,
+                                             oc.pages->as<uint8_t>(), c->st);
+                }
+            } else if (ty == HJ_VARCHAR) {
+                if (d.type == HJ_INT32 && non_null_through(in, cr) > 0)
+                    throw Error(HJ_ERR_RUNTIME, "not string or null");
+                if (d.type == HJ_VARCHAR && rows > 0) {
+                    uint8_t* pages = nullptr;
+                    oc.num_pages   = write_varchar_pages(d.refs->as<uint64_t>(), d.pages->as<uint8_t>(),
+                                                         d.num_pages, rid, rows, &pages, c->pinned, c->st);
+                    oc.pages       = std::make_shared<DevBuf>(static_cast<void*>(pages), c->st);
+                }
+                // an INT32 column that is all NULL, declared VARCHAR: all-NULL pages
+                if (d.type == HJ_INT32 && rows > 0) {
+                    Buf zero = make_buf(std::max<uint64_t>(d.rows, 1) * 8, c->st);
+                    HJ_CUDA(cudaMemsetAsync(zero->p, 0, std::max<uint64_t>(d.rows, 1) * 8, c->st));
+                    uint8_t* pages = nullptr;
+                    oc.num_pages   = write_varchar_pages(zero->as<uint64_t>(), nullptr, 0, rid, rows, &pages,
+                                                         c->pinned, c->st);
+                    oc.pages       = std::make_shared<DevBuf>(static_cast<void*>(pages), c->st);
+                }
+            }
+            res->cols.push_back(std::move(oc));
+        }
+        // ColumnarTable::num_rows = rows of the first result column (execute.cpp:437)
+        if (root.num_attrs == 0) {
+            res->num_rows = 0;
+        } else {
+            const ColRef& cr = in.cols[0];
+            DevColumn&    d  = column(cr.table, cr.col);
+            res->num_rows    = in.srcs[cr.src].rid ? in.rows : d.rows;
+        }
+    }
+};
+
+int set_err(hj_context* c, const Error& e) {
+    if (c) c->err = e.what();
+    return e.status;
+}
+
+template <class F>
+int guarded(hj_context* c, F&& f) {
+    try {
+        if (c) HJ_CUDA(cudaSetDevice(c->device));
+        f();
+        return HJ_OK;
+    } catch (const Error& e) {
+        return set_err(c, e);
+    } catch (const std::bad_alloc&) {
+        if (c) c->err = "host allocation failed";
+        return HJ_ERR_NOMEM;
+    } catch (const std::exception& e) {
+        if (c) c->err = e.what();
+        return HJ_ERR_INVALID;
+    }
+}
+
+}  // namespace
+}  // namespace hj
+
+// ===================================================================== C ABI
+
+extern "C" {
+
+const char* hj_version(void) { return "hjgb300 0.1 (sm_103a)"; }
+
+void* hj_context_stream(hj_context* c) { return c ? static_cast<void*>(c->st) : nullptr; }
+
+hj_context* hj_context_create(int device) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        hj::g_create_error = "no CUDA device available";
+        return nullptr;
+    }
+    auto* c = new hj_context();
+    try {
+        if (device < 0) HJ_CUDA(cudaGetDevice(&device));
+        if (device >= n) throw hj::Error(HJ_ERR_NO_DEVICE, "device index out of range");
+        c->device = device;
+        HJ_CUDA(cudaSetDevice(device));
+        HJ_CUDA(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
+        cudaMemPool_t mp;
+        HJ_CUDA(cudaDeviceGetDefaultMemPool(&mp, device));
+        uint64_t keep = ~0ull;  // keep freed blocks for reuse
+        HJ_CUDA(cudaMemPoolSetAttribute(mp, cudaMemPoolAttrReleaseThreshold, &keep));
+        HJ_CUDA(cudaMallocHost(&c->pinned, 64 * sizeof(uint64_t)));
+        const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+        c->pool           = std::make_unique<hj::ThreadPool>(std::min(hw, 16u) - 1);
+    } catch (const hj::Error& e) {
+        hj::g_create_error = e.what();
+        hj_context_destroy(c);
+        return nullptr;
+    }
+    return c;
+}
+
+void hj_context_destroy(hj_context* c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    c->resident.clear();
+    if (c->st) cudaStreamSynchronize(c->st);
+    for (auto e : c->slot_ev)
+        if (e) cudaEventDestroy(e);
+    if (c->staging) cudaFreeHost(c->staging);
+    if (c->pinned) cudaFreeHost(c->pinned);
+    c->pool.reset();
+    if (c->st) cudaStreamDestroy(c->st);
+    delete c;
+}
+
+const char* hj_last_error(const hj_context* c) {
+    return c ? c->err.c_str() : hj::g_create_error.c_str();
+}
+
+int hj_set_option(hj_context* c, const char* name, int64_t v) {
+    if (!c || !name) return HJ_ERR_INVALID;
+    const std::string n = name;
+    if (n == "dir_bits") c->dir_bits = v;
+    else if (n == "radix_bits") c->radix_bits = v;
+    else if (n == "probe_group") {
+        if (v != 1 && v != 4 && v != 8 && v != 32) return HJ_ERR_INVALID;
+        c->probe_group = v;
+    } else if (n == "light_max") {
+        if (v < 1) return HJ_ERR_INVALID;
+        c->light_max = v;
+    } else if (n == "timing") {
+        c->timing = v != 0;
+    } else {
+        c->err = "unknown option " + n;
+        return HJ_ERR_INVALID;
+    }
+    return HJ_OK;
+}
+
+int hj_get_option(const hj_context* c, const char* name, int64_t* v) {
+    if (!c || !name || !v) return HJ_ERR_INVALID;
+    const std::string n = name;
+    if (n == "dir_bits") *v = c->dir_bits;
+    else if (n == "radix_bits") *v = c->radix_bits;
+    else if (n == "probe_group") *v = c->probe_group;
+    else if (n == "light_max") *v = c->light_max;
+    else if (n == "timing") *v = c->timing;
+    else return HJ_ERR_INVALID;
+    return HJ_OK;
+}
+
+int hj_table_upload(hj_context* c, const hj_table_desc* t, uint64_t* handle) {
+    if (!c || !t || !handle) return HJ_ERR_INVALID;
+    return hj::guarded(c, [&] {
+        auto dt = hj::upload_table(c, *t, {});
+        HJ_CUDA(cudaStreamSynchronize(c->st));
+        const uint64_t h = c->next_handle++;
+        c->resident[h]   = dt;
+        *handle          = h;
+    });
+}
+
+int hj_table_release(hj_context* c, uint64_t handle) {
+    if (!c) return HJ_ERR_INVALID;
+    return hj::guarded(c, [&] {
+        if (!c->resident.erase(handle)) throw hj::Error(HJ_ERR_INVALID, "unknown table handle");
+        HJ_CUDA(cudaStreamSynchronize(c->st));
+    });
+}
+
+int hj_execute(hj_context* c, const hj_plan_desc* plan, hj_result** out) {
+    if (!c || !plan || !out) return HJ_ERR_INVALID;
+    *out = nullptr;
+    auto* res = new hj_result();
+    const uint64_t launches0 = hj::g_kernel_launches.load();
+    const int rc = hj::guarded(c, [&] {
+        if (plan->root >= plan->num_nodes) throw hj::Error(HJ_ERR_INVALID, "plan root out of range");
+        hj::Exec ex{c, *plan, {}};
+        // which (table, column) pairs do the scans read?
+        std::vector<std::vector<bool>> want(plan->num_inputs);
+        for (uint32_t i = 0; i < plan->num_inputs; ++i) {
+            const hj_table_desc& t = plan->inputs[i];
+            want[i].assign(t.resident ? 0 : t.num_columns, false);
+        }
+        for (uint32_t i = 0; i < plan->num_nodes; ++i) {
+            const hj_node_desc& n = plan->nodes[i];
+            if (n.kind != HJ_NODE_SCAN) continue;
+            if (n.base_table_id >= plan->num_inputs) throw hj::Error(HJ_ERR_INVALID, "scan table out of range");
+            const hj_table_desc& t = plan->inputs[n.base_table_id];
+            for (uint32_t a = 0; a < n.num_attrs; ++a) {
+                const uint64_t col = n.attrs[a].index;
+                if (t.resident) continue;
+                if (col >= t.num_columns) throw hj::Error(HJ_ERR_INVALID, "scan column out of range");
+                want[n.base_table_id][col] = true;
+            }
+        }
+        ex.phase("upload");
+        for (uint32_t i = 0; i < plan->num_inputs; ++i) {
+            const hj_table_desc& t = plan->inputs[i];
+            if (t.resident) {
+                auto it = c->resident.find(t.resident);
+                if (it == c->resident.end()) throw hj::Error(HJ_ERR_INVALID, "unknown resident table");
+                // decoded state is per call: copy the column records, share the pages
+                auto dt = std::make_shared<hj::DevTable>(*it->second);
+                for (auto& col : dt->cols) {
+                    col.decoded = false;
+                    col.vals = col.valid = col.refs = nullptr;
+                }
+                ex.tables.push_back(dt);
+            } else {
+                ex.tables.push_back(hj::upload_table(c, t, want[i]));
+            }
+        }
+        // copy_scan of every scanned column, before any join (execute.cpp:575-582)
+        ex.phase("decode");
+        for (uint32_t i = 0; i < plan->num_nodes; ++i) {
+            const hj_node_desc& n = plan->nodes[i];
+            if (n.kind != HJ_NODE_SCAN) continue;
+            for (uint32_t a = 0; a < n.num_attrs; ++a) {
+                if (n.attrs[a].index >= ex.tables[n.base_table_id]->cols.size())
+                    throw hj::Error(HJ_ERR_INVALID, "scan column out of range");
+                ex.column(uint32_t(n.base_table_id), uint32_t(n.attrs[a].index));
+            }
+        }
+        hj::Inter root = ex.run(plan->root);
+        ex.materialize(root, plan->nodes[plan->root], res);
+        ex.collect(res->phase_ms);
+        HJ_CUDA(cudaStreamSynchronize(c->st));
+        res->build_tuples = ex.build_tuples;
+        res->probe_tuples = ex.probe_tuples;
+        res->output_rows  = ex.out_rows;
+    });
+    res->kernel_launches = hj::g_kernel_launches.load() - launches0;
+    if (rc != HJ_OK) {
+        delete res;
+        cudaStreamSynchronize(c->st);
+        return rc;
+    }
+    *out = res;
+    return HJ_OK;
+}
+
+int hj_result_shape(const hj_result* r, uint64_t* num_rows, uint32_t* num_columns) {
+    if (!r) return HJ_ERR_INVALID;
+    if (num_rows) *num_rows = r->num_rows;
+    if (num_columns) *num_columns = uint32_t(r->cols.size());
+    return HJ_OK;
+}
+
+int hj_result_column(const hj_result* r, uint32_t col, int32_t* type, uint64_t* num_pages) {
+    if (!r || col >= r->cols.size()) return HJ_ERR_INVALID;
+    if (type) *type = r->cols[col].type;
+    if (num_pages) *num_pages = r->cols[col].num_pages;
+    return HJ_OK;
+}
+
+int hj_result_copy_pages(hj_context* c, const hj_result* r, uint32_t col, void* const* dst) {
+    if (!c || !r || col >= r->cols.size()) return HJ_ERR_INVALID;
+    return hj::guarded(c, [&] {
+        const auto& oc = r->cols[col];
+        if (oc.num_pages) hj::download_pages(c, oc.pages->as<uint8_t>(), oc.num_pages, dst, nullptr);
+    });
+}
+
+int hj_result_copy_contiguous(hj_context* c, const hj_result* r, uint32_t col, void* dst) {
+    if (!c || !r || col >= r->cols.size()) return HJ_ERR_INVALID;
+    return hj::guarded(c, [&] {
+        const auto& oc = r->cols[col];
+        if (oc.num_pages)
+            hj::download_pages(c, oc.pages->as<uint8_t>(), oc.num_pages, nullptr, static_cast<uint8_t*>(dst));
+    });
+}
+
+int hj_result_stats(const hj_result* r, uint64_t* b, uint64_t* p, uint64_t* o) {
+    if (!r) return HJ_ERR_INVALID;
+    if (b) *b = r->build_tuples;
+    if (p) *p = r->probe_tuples;
+    if (o) *o = r->output_rows;
+    return HJ_OK;
+}
+
+int hj_result_phase_ms(const hj_result* r, const char* phase, double* ms) {
+    if (!r || !phase || !ms) return HJ_ERR_INVALID;
+    if (std::string(phase) == "launches") {
+        *ms = double(r->kernel_launches);
+        return HJ_OK;
+    }
+    auto it = r->phase_ms.find(phase);
+    *ms     = it == r->phase_ms.end() ? 0.0 : it->second;
+    return HJ_OK;
+}
+
+void hj_result_free(hj_result* r) { delete r; }
+
+// ---- hash table on device columns ----------------------------------------
+
+int hj_table_build(hj_context* c, const int32_t* keys, const uint32_t* valid, uint64_t n,
+                   int32_t dir_bits, hj_hash_table** out) {
+    if (!c || !out || (n > 0 && !keys)) return HJ_ERR_INVALID;
+    *out = nullptr;
+    auto* ht = new hj_hash_table();
+    ht->st   = c->st;
+    const int rc = hj::guarded(c, [&] {
+        if (n > 0xffffffffull) throw hj::Error(HJ_ERR_INVALID, "more than 2^32 build rows");
+        hj::KeyCol kc{keys, valid, nullptr, n};
+        hj::build_table(kc, dir_bits, int(c->radix_bits), ht->t, c->pinned, c->st);
+        HJ_CUDA(cudaStreamSynchronize(c->st));
+    });
+    if (rc != HJ_OK) {
+        delete ht;
+        return rc;
+    }
+    *out = ht;
+    return HJ_OK;
+}
+
+int hj_table_info(const hj_hash_table* t, uint32_t* dir_bits, uint64_t* num_tuples, const uint64_t** dir,
+                  const int32_t** keys, const uint32_t** rows) {
+    if (!t) return HJ_ERR_INVALID;
+    if (dir_bits) *dir_bits = t->t.dir_bits;
+    if (num_tuples) *num_tuples = t->t.n_tuples;
+    if (dir) *dir = t->t.dir;
+    if (keys) *keys = t->t.keys;
+    if (rows) *rows = t->t.rows;
+    return HJ_OK;
+}
+
+int hj_table_probe(hj_context* c, const hj_hash_table* t, const int32_t* keys, const uint32_t* valid,
+                   uint64_t n, uint32_t* out_probe, uint32_t* out_build, uint64_t capacity,
+                   uint64_t* num_matches) {
+    if (!c || !t || !num_matches || (n > 0 && !keys)) return HJ_ERR_INVALID;
+    int status = HJ_OK;
+    const int rc = hj::guarded(c, [&] {
+        if (n > 0xffffffffull) throw hj::Error(HJ_ERR_INVALID, "more than 2^32 probe rows");
+        hj::KeyCol      pk{keys, valid, nullptr, n};
+        hj::ProbeParams prm;
+        prm.light_max = int(c->light_max);
+        prm.group     = int(c->probe_group);
+        prm.pinned    = c->pinned;
+        hj::ProbePlan* pp = nullptr;
+        try {
+            const uint64_t total = hj::probe_count(t->t, pk, prm, &pp, c->st);
+            *num_matches         = total;
+            if (total > capacity) {
+                status = HJ_ERR_CAPACITY;
+            } else if (total > 0) {
+                if (!out_probe || !out_build) throw hj::Error(HJ_ERR_INVALID, "null output buffer");
+                hj::RidOut ro[2] = {{0, nullptr, out_probe}, {1, nullptr, out_build}};
+                hj::probe_write(t->t, pk, pp, ro, 2, c->st);
+            }
+        } catch (...) {
+            hj::probe_free(pp, c->st);
+            throw;
+        }
+        hj::probe_free(pp, c->st);
+        HJ_CUDA(cudaStreamSynchronize(c->st));
+    });
+    if (rc != HJ_OK) return rc;
+    if (status != HJ_OK) c->err = "output capacity too small";
+    return status;
+}
+
+void hj_table_free(hj_hash_table* t) {
+    if (!t) return;
+    hj::free_table(t->t, t->st);
+    cudaStreamSynchronize(t->st);
+    delete t;
+}
+
+}  // extern "C"

@@ -1,0 +1,106 @@
+// Host launchers of the engine's CUDA kernels.  Every launcher enqueues on
+// `st` and does not synchronise; device pointers only.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace hj {
+
+// Stream-ordered device memory (cudaMallocAsync on a pool that keeps freed
+// blocks cached for reuse).
+void* dalloc(size_t bytes, cudaStream_t st);
+void  dfree(void* p, cudaStream_t st);
+
+template <class T>
+T* dalloc_n(size_t n, cudaStream_t st) {
+    return static_cast<T*>(dalloc(n * sizeof(T) + 16, st));
+}
+
+// ---- scans (hj_scan.cu) ---------------------------------------------------
+// out[i] = sum(in[0..i)), out[n] = total.  out has n + 1 slots.
+void scan_exclusive_u32_to_u64(const uint32_t* in, uint64_t* out, uint64_t n, cudaStream_t st);
+void scan_exclusive_u64(const uint64_t* in, uint64_t* out, uint64_t n, cudaStream_t st);
+
+// ---- page decode (hj_decode.cu) --------------------------------------------
+// Per page: rows it contributes to its column (0xfffe pages: 0, 0xffff: 1),
+// non-NULL rows, and flags (bit 0: page has NULLs; bit 1: page index exceeds
+// the 18-bit StrRef field and carries strings).
+void launch_page_headers(const uint8_t* pages, uint64_t num_pages, int32_t type,
+                         uint32_t* rows, uint32_t* non_null, uint32_t* flags, cudaStream_t st);
+// INT32 pages -> values + validity bitmap (bitmap pre-zeroed, or nullptr when the
+// column has no NULLs).  row_start: exclusive scan of page rows.
+void launch_decode_int32(const uint8_t* pages, uint64_t num_pages, const uint64_t* row_start,
+                         int32_t* vals, uint32_t* valid, cudaStream_t st);
+// VARCHAR pages -> value_t per row (StrRef(table, column, page, ordinal) or 0 =
+// NULL) + validity bitmap (pre-zeroed).
+void launch_decode_varchar(const uint8_t* pages, uint64_t num_pages, const uint64_t* row_start,
+                           uint32_t table_id, uint32_t column, uint64_t* refs, uint32_t* valid,
+                           cudaStream_t st);
+
+// ---- unchained table build (hj_build.cu) -----------------------------------
+struct KeyCol {
+    const int32_t*  vals;   // values of the base column
+    const uint32_t* valid;  // validity bitmap of the base column or nullptr
+    const uint32_t* rid;    // row ids into the base column, or nullptr = identity
+    uint64_t        n;      // rows of the (intermediate) column
+};
+
+struct Table {
+    uint32_t  dir_bits  = 0;
+    uint64_t  n_tuples  = 0;
+    uint64_t* dir       = nullptr;  // 2^dir_bits + 1 words: start << 16 | bloom
+    int32_t*  keys      = nullptr;  // adjacency array: keys
+    uint32_t* rows      = nullptr;  // adjacency array: build row ids (index into KeyCol)
+    uint32_t* mixed     = nullptr;  // bit p set: bucket p holds more than one distinct key
+};
+
+// Builds `t` over the valid keys of `kc`.  dir_bits < 0: next_pow2(#valid).
+// radix_bits < 0: automatic.  Allocates t's arrays with dalloc.  Synchronises
+// once (to size the directory).
+void build_table(const KeyCol& kc, int dir_bits, int radix_bits, Table& t, uint64_t* scratch_host,
+                 cudaStream_t st);
+void free_table(Table& t, cudaStream_t st);
+
+// ---- probe (hj_probe.cu) ---------------------------------------------------
+// One output row-id stream of a join: out[k] = src ? src[x] : x, where x is the
+// probe row (side 0) or the build row (side 1) of match k.
+struct RidOut {
+    int             side;
+    const uint32_t* src;
+    uint32_t*       dst;
+};
+constexpr int kMaxRidOut = 16;
+
+struct ProbeParams {
+    int       light_max = 32;       // larger buckets are not scanned by one thread
+    int       group     = 8;        // threads per probe key in the write pass (1, 4, 8, 32)
+    uint64_t* pinned    = nullptr;  // >= 8 words of pinned host memory for count readback
+};
+
+struct ProbePlan;  // opaque match list between the count and write passes
+
+// Count pass: returns the number of matches; keeps the hit list in *pp.
+uint64_t probe_count(const Table& t, const KeyCol& pk, const ProbeParams& prm, ProbePlan** pp,
+                     cudaStream_t st);
+// Write pass: emits the row-id streams for the matches found by probe_count
+// (all `nout` streams have probe_count() slots) and frees *pp.
+void probe_write(const Table& t, const KeyCol& pk, ProbePlan* pp, const RidOut* outs, int nout,
+                 cudaStream_t st);
+void probe_free(ProbePlan* pp, cudaStream_t st);
+
+// ---- output pages (hj_materialize.cu) --------------------------------------
+// INT32 output column of n rows gathered through rid (nullptr = identity) from a
+// base column; writes ceil(n / 1984) pages.
+void launch_write_int32_pages(const int32_t* vals, const uint32_t* valid, const uint32_t* rid,
+                              uint64_t n, uint8_t* out_pages, cudaStream_t st);
+
+// VARCHAR output column: returns the number of pages and writes them into a
+// buffer it allocates (*out_pages, freed by the caller with dfree).
+// `pinned`: >= 2 words of pinned host memory (page-count readback).
+uint64_t write_varchar_pages(const uint64_t* refs, const uint8_t* base_pages,
+                             uint64_t base_num_pages, const uint32_t* rid, uint64_t n,
+                             uint8_t** out_pages, uint64_t* pinned, cudaStream_t st);
+
+}  // namespace hj

@@ -1,0 +1,399 @@
+// Probe of the unchained table on the GPU.
+//
+// Semantics of UnchainedHash::probe (include/unchained.h:220-246 of the
+// reference) applied to a column of probe keys, as the reference's probe
+// workers do (src/execute.cpp:111-165): NULL keys never match (:127-129),
+// Bloom early-reject on the directory word, then every tuple of the bucket
+// with an equal key is a match.
+//
+// Count pass (k_probe_count): each block walks 2048-row tiles.  A probe key
+// reads its directory word, rejects on the Bloom tag, and classifies the hit:
+//   light  bucket of <= light_max tuples (or a single tuple): counted by key
+//          compare; staged in shared memory via warp ballot/popc and flushed
+//          with ONE global atomic per tile (the reference's per-thread
+//          work-stealing counter becomes this per-block reservation);
+//   big    larger bucket whose tuples all carry one key (the per-bucket
+//          "mixed" bit is clear): the whole bucket matches or nothing does,
+//          so the count is the bucket size without reading it;
+//   mixed  larger bucket with several keys: counted by a whole block
+//          (k_mixed_count).
+// Write pass: prefix sums of the counts give each hit its output slot; light
+// hits are expanded by groups of `group` threads, big hits in 16K-tuple units
+// spread over all SMs (one Zipf-heavy key can own millions of tuples), mixed
+// hits by a block each.  Every match writes one row id per requested output
+// stream, composed through the sides' row-id vectors (late materialisation).
+#include <algorithm>
+
+#include "hj_block.cuh"
+#include "hj_common.cuh"
+#include "hj_kernels.h"
+
+namespace hj {
+
+namespace {
+
+constexpr int      kPT      = 256;
+constexpr int      kPI      = 8;
+constexpr int      kPTile   = kPT * kPI;
+constexpr uint32_t kSplit   = 16384;  // tuples per big-hit work unit
+
+struct ProbeTab {
+    const uint64_t* dir;
+    const int32_t*  keys;
+    const uint32_t* rows;
+    const uint32_t* mixed;
+    uint32_t        b;
+};
+
+struct Lists {
+    uint32_t *l_row, *l_s, *l_cnt;
+    int32_t*  l_key;
+    uint32_t *b_row, *b_s, *b_e;
+    uint32_t *m_row, *m_s, *m_e, *m_cnt;
+    int32_t*  m_key;
+    unsigned long long* ctr;  // 0 n_light, 1 n_big, 2 n_mixed, 3 tot_light, 4 tot_big, 5 tot_mixed
+};
+
+struct Outs {
+    int    n;
+    RidOut o[kMaxRidOut];
+};
+
+__device__ __forceinline__ void emit(const Outs& outs, uint64_t pos, uint32_t prow, uint32_t brow) {
+#pragma unroll 4
+    for (int i = 0; i < outs.n; ++i) {
+        const RidOut& o = outs.o[i];
+        const uint32_t x = o.side == 0 ? prow : brow;
+        o.dst[pos]       = o.src ? __ldg(o.src + x) : x;
+    }
+}
+
+__global__ void __launch_bounds__(kPT)
+    k_probe_count(ProbeTab T, KeyCol pk, int light_max, Lists Ls, uint64_t ntiles) {
+    __shared__ uint32_t s_row[kPTile], s_s[kPTile], s_cnt[kPTile];
+    __shared__ int32_t  s_key[kPTile];
+    __shared__ uint32_t s_n, s_base;
+    __shared__ unsigned long long s_red[33];
+    const unsigned lane = threadIdx.x & 31;
+    uint64_t       tot_light = 0, tot_big = 0;
+    for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        if (threadIdx.x == 0) s_n = 0;
+        __syncthreads();
+#pragma unroll 2
+        for (int it = 0; it < kPI; ++it) {
+            const uint64_t j   = tile * kPTile + uint64_t(it) * kPT + threadIdx.x;
+            int            cls = 0;  // 0 miss, 1 light, 2 big, 3 mixed
+            uint32_t       c = 0, s = 0, e = 0;
+            int32_t        key = 0;
+            if (j < pk.n) {
+                const uint64_t r = pk.rid ? uint64_t(__ldg(pk.rid + j)) : j;
+                if (bit_valid(pk.valid, r)) {
+                    key                = __ldg(pk.vals + r);
+                    const uint64_t h   = fib_hash(key);
+                    const uint64_t p   = bucket_of(h, T.b);
+                    const uint64_t w   = __ldg(T.dir + p);
+                    const uint32_t m   = bloom_mask(h);
+                    if ((uint32_t(w) & m) == m) {
+                        s                = uint32_t(w >> 16);
+                        e                = uint32_t(__ldg(T.dir + p + 1) >> 16);
+                        const uint32_t L = e - s;
+                        const int32_t  k0 = __ldg(T.keys + s);
+                        if (L == 1) {
+                            c   = k0 == key;
+                            cls = c ? 1 : 0;
+                        } else if (!((__ldg(T.mixed + (p >> 5)) >> (p & 31)) & 1u)) {
+                            c   = k0 == key ? L : 0;
+                            cls = c ? (L <= uint32_t(light_max) ? 1 : 2) : 0;
+                        } else if (L <= uint32_t(light_max)) {
+                            for (uint32_t k = s; k < e; ++k) c += __ldg(T.keys + k) == key;
+                            cls = c ? 1 : 0;
+                        } else {
+                            cls = 3;
+                        }
+                    }
+                }
+            }
+            // light: stage in shared memory
+            {
+                const unsigned bal = __ballot_sync(0xffffffffu, cls == 1);
+                uint32_t       base = 0;
+                if (lane == 0 && bal) base = atomicAdd(&s_n, uint32_t(__popc(bal)));
+                base = __shfl_sync(0xffffffffu, base, 0);
+                if (cls == 1) {
+                    const uint32_t q = base + __popc(bal & ((1u << lane) - 1));
+                    s_row[q]         = uint32_t(j);
+                    s_s[q]           = s;
+                    s_cnt[q]         = c;
+                    s_key[q]         = key;
+                    tot_light += c;
+                }
+            }
+            // big / mixed: rare, warp-aggregated global atomics
+            {
+                const unsigned bal = __ballot_sync(0xffffffffu, cls == 2);
+                if (bal) {
+                    unsigned long long base = 0;
+                    if (lane == 0) base = atomicAdd(Ls.ctr + 1, (unsigned long long)__popc(bal));
+                    base = __shfl_sync(0xffffffffu, base, 0);
+                    if (cls == 2) {
+                        const uint64_t q = base + __popc(bal & ((1u << lane) - 1));
+                        Ls.b_row[q]      = uint32_t(j);
+                        Ls.b_s[q]        = s;
+                        Ls.b_e[q]        = e;
+                        tot_big += c;
+                    }
+                }
+            }
+            {
+                const unsigned bal = __ballot_sync(0xffffffffu, cls == 3);
+                if (bal) {
+                    unsigned long long base = 0;
+                    if (lane == 0) base = atomicAdd(Ls.ctr + 2, (unsigned long long)__popc(bal));
+                    base = __shfl_sync(0xffffffffu, base, 0);
+                    if (cls == 3) {
+                        const uint64_t q = base + __popc(bal & ((1u << lane) - 1));
+                        Ls.m_row[q]      = uint32_t(j);
+                        Ls.m_s[q]        = s;
+                        Ls.m_e[q]        = e;
+                        Ls.m_key[q]      = key;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) s_base = uint32_t(atomicAdd(Ls.ctr + 0, (unsigned long long)s_n));
+        __syncthreads();
+        const uint32_t nst = s_n, gb = s_base;
+        for (uint32_t q = threadIdx.x; q < nst; q += blockDim.x) {
+            Ls.l_row[gb + q] = s_row[q];
+            Ls.l_s[gb + q]   = s_s[q];
+            Ls.l_cnt[gb + q] = s_cnt[q];
+            Ls.l_key[gb + q] = s_key[q];
+        }
+        __syncthreads();
+    }
+    unsigned long long t1, t2;
+    block_exclusive_scan<unsigned long long>(tot_light, s_red, &t1);
+    block_exclusive_scan<unsigned long long>(tot_big, s_red, &t2);
+    if (threadIdx.x == 0) {
+        if (t1) atomicAdd(Ls.ctr + 3, t1);
+        if (t2) atomicAdd(Ls.ctr + 4, t2);
+    }
+}
+
+__global__ void __launch_bounds__(512) k_mixed_count(ProbeTab T, Lists Ls) {
+    __shared__ unsigned long long s_red[33];
+    const uint64_t n   = Ls.ctr[2];
+    uint64_t       acc = 0;
+    for (uint64_t q = blockIdx.x; q < n; q += gridDim.x) {
+        const uint32_t s = Ls.m_s[q], e = Ls.m_e[q];
+        const int32_t  key = Ls.m_key[q];
+        unsigned long long c = 0;
+        for (uint32_t k = s + threadIdx.x; k < e; k += blockDim.x) c += __ldg(T.keys + k) == key;
+        unsigned long long tot;
+        block_exclusive_scan<unsigned long long>(c, s_red, &tot);
+        if (threadIdx.x == 0) {
+            Ls.m_cnt[q] = uint32_t(tot);
+            acc += tot;
+        }
+    }
+    if (threadIdx.x == 0 && acc) atomicAdd(Ls.ctr + 5, (unsigned long long)acc);
+}
+
+__global__ void k_big_units(const uint32_t* __restrict__ b_s, const uint32_t* __restrict__ b_e,
+                            uint64_t n, uint32_t* __restrict__ units, uint32_t* __restrict__ lens) {
+    const uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t L = b_e[i] - b_s[i];
+    lens[i]          = L;
+    units[i]         = (L + kSplit - 1) / kSplit;
+}
+
+template <int G>
+__global__ void __launch_bounds__(256)
+    k_write_light(ProbeTab T, Lists Ls, uint64_t n_light, const uint64_t* __restrict__ off, Outs outs) {
+    const unsigned lane = threadIdx.x & 31;
+    const unsigned grp  = lane / G, gl = lane % G;
+    const unsigned gmask = G == 32 ? 0xffffffffu : ((1u << G) - 1) << (grp * G);
+    const uint64_t warp   = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = (uint64_t(gridDim.x) * blockDim.x) >> 5;
+    constexpr int  HPW    = 32 / G;  // hits per warp step
+    for (uint64_t hb = warp * HPW; hb < n_light; hb += nwarps * HPW) {
+        const uint64_t h    = hb + grp;
+        const bool     have = h < n_light;
+        uint32_t       s = 0, L = 0, prow = 0;
+        int32_t        key = 0;
+        uint64_t       pos = 0;
+        if (have) {
+            s    = Ls.l_s[h];
+            prow = Ls.l_row[h];
+            key  = Ls.l_key[h];
+            pos  = off[h];
+            // the bucket end is the next directory word's start; recompute it
+            const uint64_t p = bucket_of(fib_hash(key), T.b);
+            L                = uint32_t(__ldg(T.dir + p + 1) >> 16) - s;
+        }
+        for (uint32_t k0 = 0; __any_sync(0xffffffffu, have && k0 < L); k0 += G) {
+            const uint32_t k  = s + k0 + gl;
+            const bool     m  = have && k0 + gl < L && __ldg(T.keys + k) == key;
+            const unsigned bl = __ballot_sync(0xffffffffu, m) & gmask;
+            if (m) emit(outs, pos + __popc(bl & ((1u << lane) - 1)), prow, __ldg(T.rows + k));
+            pos += __popc(bl);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256)
+    k_write_big(ProbeTab T, Lists Ls, uint64_t n_big, const uint64_t* __restrict__ unit_off,
+                const uint64_t* __restrict__ big_off, uint64_t base_pos, Outs outs) {
+    const uint64_t nunits = unit_off[n_big];
+    for (uint64_t u = blockIdx.x; u < nunits; u += gridDim.x) {
+        uint64_t lo = 0, hi = n_big;  // largest h with unit_off[h] <= u
+        while (hi - lo > 1) {
+            const uint64_t mid = (lo + hi) >> 1;
+            if (unit_off[mid] <= u) lo = mid;
+            else                    hi = mid;
+        }
+        const uint64_t h    = lo;
+        const uint64_t sub  = u - unit_off[h];
+        const uint32_t s0   = Ls.b_s[h] + uint32_t(sub) * kSplit;
+        const uint32_t e0   = min(Ls.b_e[h], s0 + kSplit);
+        const uint32_t prow = Ls.b_row[h];
+        const uint64_t pos0 = base_pos + big_off[h] + sub * kSplit;
+        for (uint32_t k = s0 + threadIdx.x; k < e0; k += blockDim.x)
+            emit(outs, pos0 + (k - s0), prow, __ldg(T.rows + k));
+    }
+}
+
+__global__ void __launch_bounds__(512)
+    k_write_mixed(ProbeTab T, Lists Ls, const uint64_t* __restrict__ mixed_off, uint64_t base_pos,
+                  Outs outs) {
+    __shared__ uint32_t sm[33];
+    const uint64_t n = Ls.ctr[2];
+    for (uint64_t q = blockIdx.x; q < n; q += gridDim.x) {
+        const uint32_t s = Ls.m_s[q], e = Ls.m_e[q], prow = Ls.m_row[q];
+        const int32_t  key = Ls.m_key[q];
+        uint64_t       pos = base_pos + mixed_off[q];
+        for (uint32_t b = s; b < e; b += blockDim.x) {
+            const uint32_t k = b + threadIdx.x;
+            const bool     m = k < e && __ldg(T.keys + k) == key;
+            uint32_t       tot;
+            const uint32_t r = block_exclusive_scan<uint32_t>(m ? 1u : 0u, sm, &tot);
+            if (m) emit(outs, pos + r, prow, __ldg(T.rows + k));
+            pos += tot;
+        }
+    }
+}
+
+ProbeTab tab_of(const Table& t) { return ProbeTab{t.dir, t.keys, t.rows, t.mixed, t.dir_bits}; }
+
+}  // namespace
+
+struct ProbePlan {
+    Lists     ls{};
+    uint64_t  cap     = 0;
+    uint64_t  n_light = 0, n_big = 0, n_mixed = 0;
+    uint64_t  tot_light = 0, tot_big = 0, tot_mixed = 0;
+    uint64_t* host    = nullptr;  // pinned readback of the counters (owned by the caller)
+    int       group   = 8;
+};
+
+uint64_t probe_count(const Table& t, const KeyCol& pk, const ProbeParams& prm, ProbePlan** out,
+                     cudaStream_t st) {
+    auto* pp  = new ProbePlan();
+    *out      = pp;
+    pp->group = prm.group;
+    if (t.n_tuples == 0 || pk.n == 0) return 0;
+    if (pk.n > 0xffffffffull) throw Error(HJ_ERR_INVALID, "more than 2^32 probe rows");
+    const uint64_t n = pk.n;
+    pp->cap          = n;
+    Lists& L         = pp->ls;
+    L.l_row = dalloc_n<uint32_t>(n, st);
+    L.l_s   = dalloc_n<uint32_t>(n, st);
+    L.l_cnt = dalloc_n<uint32_t>(n, st);
+    L.l_key = dalloc_n<int32_t>(n, st);
+    L.b_row = dalloc_n<uint32_t>(n, st);
+    L.b_s   = dalloc_n<uint32_t>(n, st);
+    L.b_e   = dalloc_n<uint32_t>(n, st);
+    L.m_row = dalloc_n<uint32_t>(n, st);
+    L.m_s   = dalloc_n<uint32_t>(n, st);
+    L.m_e   = dalloc_n<uint32_t>(n, st);
+    L.m_cnt = dalloc_n<uint32_t>(n, st);
+    L.m_key = dalloc_n<int32_t>(n, st);
+    L.ctr   = dalloc_n<unsigned long long>(8, st);
+    HJ_CUDA(cudaMemsetAsync(L.ctr, 0, 8 * sizeof(unsigned long long), st));
+    const ProbeTab T      = tab_of(t);
+    const uint64_t ntiles = (n + kPTile - 1) / kPTile;
+    const int      grid   = int(std::min<uint64_t>(ntiles, uint64_t(kSMs) * 8));
+    k_probe_count<<<grid, kPT, 0, st>>>(T, pk, prm.light_max, L, ntiles);
+    HJ_LAUNCH_CHECK();
+    k_mixed_count<<<kSMs * 2, 512, 0, st>>>(T, L);
+    HJ_LAUNCH_CHECK();
+    pp->host = prm.pinned;
+    HJ_CUDA(cudaMemcpyAsync(pp->host, L.ctr, 6 * sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+    HJ_CUDA(cudaStreamSynchronize(st));
+    pp->n_light   = pp->host[0];
+    pp->n_big     = pp->host[1];
+    pp->n_mixed   = pp->host[2];
+    pp->tot_light = pp->host[3];
+    pp->tot_big   = pp->host[4];
+    pp->tot_mixed = pp->host[5];
+    return pp->tot_light + pp->tot_big + pp->tot_mixed;
+}
+
+void probe_write(const Table& t, const KeyCol& pk, ProbePlan* pp, const RidOut* ro, int nout,
+                 cudaStream_t st) {
+    (void)pk;
+    if (nout > kMaxRidOut) throw Error(HJ_ERR_INVALID, "too many output row-id streams");
+    Outs outs{};
+    outs.n = nout;
+    for (int i = 0; i < nout; ++i) outs.o[i] = ro[i];
+    if (pp->cap == 0 || nout == 0) return;
+    const ProbeTab T = tab_of(t);
+    Lists&         L = pp->ls;
+    if (pp->n_light) {
+        uint64_t* off = dalloc_n<uint64_t>(pp->n_light + 1, st);
+        scan_exclusive_u32_to_u64(L.l_cnt, off, pp->n_light, st);
+        const int grid = int(std::min<uint64_t>(div_up(pp->n_light, 256), uint64_t(kSMs) * 16));
+        switch (pp->group) {
+        case 1: k_write_light<1><<<grid, 256, 0, st>>>(T, L, pp->n_light, off, outs); break;
+        case 4: k_write_light<4><<<grid, 256, 0, st>>>(T, L, pp->n_light, off, outs); break;
+        case 32: k_write_light<32><<<grid, 256, 0, st>>>(T, L, pp->n_light, off, outs); break;
+        default: k_write_light<8><<<grid, 256, 0, st>>>(T, L, pp->n_light, off, outs); break;
+        }
+        HJ_LAUNCH_CHECK();
+        dfree(off, st);
+    }
+    if (pp->n_big) {
+        uint32_t* units    = dalloc_n<uint32_t>(pp->n_big, st);
+        uint32_t* lens     = dalloc_n<uint32_t>(pp->n_big, st);
+        uint64_t* unit_off = dalloc_n<uint64_t>(pp->n_big + 1, st);
+        uint64_t* big_off  = dalloc_n<uint64_t>(pp->n_big + 1, st);
+        k_big_units<<<div_up(pp->n_big, 256), 256, 0, st>>>(L.b_s, L.b_e, pp->n_big, units, lens);
+        HJ_LAUNCH_CHECK();
+        scan_exclusive_u32_to_u64(units, unit_off, pp->n_big, st);
+        scan_exclusive_u32_to_u64(lens, big_off, pp->n_big, st);
+        k_write_big<<<kSMs * 4, 256, 0, st>>>(T, L, pp->n_big, unit_off, big_off, pp->tot_light, outs);
+        HJ_LAUNCH_CHECK();
+        for (void* p : {(void*)units, (void*)lens, (void*)unit_off, (void*)big_off}) dfree(p, st);
+    }
+    if (pp->n_mixed) {
+        uint64_t* off = dalloc_n<uint64_t>(pp->n_mixed + 1, st);
+        scan_exclusive_u32_to_u64(L.m_cnt, off, pp->n_mixed, st);
+        k_write_mixed<<<kSMs * 2, 512, 0, st>>>(T, L, off, pp->tot_light + pp->tot_big, outs);
+        HJ_LAUNCH_CHECK();
+        dfree(off, st);
+    }
+}
+
+void probe_free(ProbePlan* pp, cudaStream_t st) {
+    if (!pp) return;
+    Lists& L = pp->ls;
+    for (void* p : {(void*)L.l_row, (void*)L.l_s, (void*)L.l_cnt, (void*)L.l_key, (void*)L.b_row,
+                    (void*)L.b_s, (void*)L.b_e, (void*)L.m_row, (void*)L.m_s, (void*)L.m_e,
+                    (void*)L.m_cnt, (void*)L.m_key, (void*)L.ctr})
+        if (p) dfree(p, st);
+    delete pp;
+}
+
+}  // namespace hj

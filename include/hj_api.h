@@ -1,0 +1,200 @@
+/*
+ * C ABI of the GB300 hash-join engine (libhjgb300.so).
+ *
+ * This is the flat, FFI-friendly form of the contest entry points of
+ * eleanalt/hash-join-optimizer.  Plain pointers and sizes only; no C++ or torch
+ * types cross it.  The C++ `Contest::execute(const Plan&, void*)` of
+ * include/plan.h is a thin wrapper over `hj_execute`.
+ *
+ *   reference interface (file:line in eleanalt/hash-join-optimizer)   replaced by
+ *   Contest::build_context()            include/plan.h:400, src/execute.cpp:610   hj_context_create
+ *   Contest::destroy_context(void*)     include/plan.h:401, src/execute.cpp:614   hj_context_destroy
+ *   Contest::execute(const Plan&,void*) include/plan.h:403, src/execute.cpp:598   hj_execute + hj_result_*
+ *   UnchainedHash::build_insert/finalize_build
+ *                                       include/unchained.h:155-217               hj_table_build
+ *   UnchainedHash::probe(key, cb)       include/unchained.h:220-246               hj_table_probe
+ *   PartitionedDirectoryHash::build/probe
+ *                                       include/partitioned_directory_hash.h:86-215 hj_table_build / hj_table_probe
+ *   Table::to_columnar / ColumnInserter src/build_table.cpp:657-882, plan.h:212-396 hj_pages_from_* (host)
+ *
+ * Errors: every entry point returns an HJ_* status.  The classes mirror the
+ * exceptions the reference throws: HJ_ERR_RUNTIME <-> std::runtime_error
+ * ("Join key isn't of type int32_t", src/execute.cpp:81,130), HJ_ERR_OUT_OF_RANGE
+ * <-> std::out_of_range (StrRef field overflow, include/value_t.h:36-47).
+ * hj_last_error() gives the message of the last failure on a context.
+ *
+ * Threading: a context is used by one host thread at a time, as the contest
+ * harness calls execute() (tests/read_sql.cpp:1434-1447).  All device work of a
+ * context runs in order on the context's CUDA stream.
+ */
+#ifndef HJ_API_H
+#define HJ_API_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HJ_PAGE_SIZE 8192
+
+enum hj_status {
+    HJ_OK                = 0,
+    HJ_ERR_INVALID       = 1, /* malformed plan or argument                     */
+    HJ_ERR_RUNTIME       = 2, /* std::runtime_error class                       */
+    HJ_ERR_OUT_OF_RANGE  = 3, /* std::out_of_range class (StrRef overflow)      */
+    HJ_ERR_CUDA          = 4, /* a CUDA runtime call failed                     */
+    HJ_ERR_NO_DEVICE     = 5, /* no usable CUDA device                          */
+    HJ_ERR_CAPACITY      = 6, /* caller buffer too small; size needed returned  */
+    HJ_ERR_DEVICE_STATUS = 7, /* a kernel reported an error in its status word  */
+    HJ_ERR_NOMEM         = 8  /* device or pinned host allocation failed        */
+};
+
+/* DataType enumerators in the order of `enum class DataType`. */
+enum hj_dtype { HJ_INT32 = 0, HJ_INT64 = 1, HJ_FP64 = 2, HJ_VARCHAR = 3 };
+
+/* NodeType enumerators in the order of `enum class NodeType`. */
+enum hj_node_kind { HJ_NODE_JOIN = 0, HJ_NODE_SCAN = 1 };
+
+/* One input column: `num_pages` pointers to 8192-byte pages in host memory. */
+typedef struct hj_column_desc {
+    int32_t            type;      /* hj_dtype */
+    uint64_t           num_pages;
+    const void* const* pages;
+} hj_column_desc;
+
+/* One input table.  `resident` = 0: the pages above are host pages, uploaded
+ * per call.  Otherwise it is a handle from hj_table_upload() and the table is
+ * read from HBM (columns/num_columns are then ignored). */
+typedef struct hj_table_desc {
+    uint64_t              num_rows;
+    uint32_t              num_columns;
+    const hj_column_desc* columns;
+    uint64_t              resident;
+} hj_table_desc;
+
+/* One (column index, DataType) entry of PlanNode::output_attrs. */
+typedef struct hj_attr {
+    uint64_t index;
+    int32_t  type;
+} hj_attr;
+
+/* PlanNode.  kind = HJ_NODE_SCAN uses base_table_id; kind = HJ_NODE_JOIN uses
+ * build_left/left/right/left_attr/right_attr with the meaning of JoinNode. */
+typedef struct hj_node_desc {
+    int32_t        kind;
+    int32_t        build_left;
+    uint64_t       base_table_id;
+    uint64_t       left;
+    uint64_t       right;
+    uint64_t       left_attr;
+    uint64_t       right_attr;
+    uint32_t       num_attrs;
+    const hj_attr* attrs;
+} hj_node_desc;
+
+typedef struct hj_plan_desc {
+    uint32_t             num_nodes;
+    const hj_node_desc*  nodes;
+    uint32_t             num_inputs;
+    const hj_table_desc* inputs;
+    uint64_t             root;
+} hj_plan_desc;
+
+typedef struct hj_context    hj_context;
+typedef struct hj_result     hj_result;
+typedef struct hj_hash_table hj_hash_table;
+
+/* ---- context (Contest::build_context / destroy_context) ------------------ */
+
+/* Creates a context on CUDA device `device` (-1 = current device).  Returns
+ * NULL when no device is usable; hj_last_error(NULL) then says why. */
+hj_context* hj_context_create(int device);
+void        hj_context_destroy(hj_context* ctx);
+/* Message of the last failed call on `ctx` (or of the last failed create). */
+const char* hj_last_error(const hj_context* ctx);
+/* Library version string. */
+const char* hj_version(void);
+/* The cudaStream_t all device work of the context runs on (for callers that
+ * order their own work or CUDA events against it). */
+void* hj_context_stream(hj_context* ctx);
+
+/* Engine tunables.  Names: "dir_bits" (-1 = next_pow2 of the build tuples, as
+ * UnchainedHash::choose_directory_size), "radix_bits" (partition fan-out of the
+ * build, 0..12), "probe_group" (threads per probe key: 1, 4, 8 or 32),
+ * "light_max" (largest bucket scanned by one probe group before the bucket is
+ * handed to a whole block), "timing" (1: record per-phase device times of
+ * each hj_execute, read with hj_result_phase_ms). */
+int hj_set_option(hj_context* ctx, const char* name, int64_t value);
+int hj_get_option(const hj_context* ctx, const char* name, int64_t* value);
+
+/* ---- resident base tables (HBM) ------------------------------------------ */
+
+/* Uploads a host table once and keeps its pages in HBM; returns a handle for
+ * hj_table_desc.resident.  hj_table_release frees it. */
+int hj_table_upload(hj_context* ctx, const hj_table_desc* table, uint64_t* handle);
+int hj_table_release(hj_context* ctx, uint64_t handle);
+
+/* ---- query execution (Contest::execute) ---------------------------------- */
+
+/* Runs the plan.  On success *out holds the root's columns as pages in HBM;
+ * fetch them with hj_result_copy_pages, free with hj_result_free. */
+int hj_execute(hj_context* ctx, const hj_plan_desc* plan, hj_result** out);
+
+int hj_result_shape(const hj_result* res, uint64_t* num_rows, uint32_t* num_columns);
+int hj_result_column(const hj_result* res, uint32_t col, int32_t* type, uint64_t* num_pages);
+/* Copies the pages of column `col` to host memory: page i goes to dst_pages[i]
+ * (8192 bytes each; no alignment needed). */
+int hj_result_copy_pages(hj_context* ctx, const hj_result* res, uint32_t col,
+                         void* const* dst_pages);
+/* Same, into one contiguous host buffer of num_pages * 8192 bytes. */
+int hj_result_copy_contiguous(hj_context* ctx, const hj_result* res, uint32_t col, void* dst);
+/* Kernel-side statistics of the last hj_execute on this result: number of
+ * build tuples, probe tuples and output rows summed over all joins. */
+int  hj_result_stats(const hj_result* res, uint64_t* build_tuples, uint64_t* probe_tuples,
+                     uint64_t* output_rows);
+/* Device milliseconds of one phase of the hj_execute that made `res` (option
+ * "timing" = 1): "upload", "decode", "build", "probe", "materialize", "total".
+ * Phase "launches" gives the number of kernels that hj_execute launched. */
+int  hj_result_phase_ms(const hj_result* res, const char* phase, double* ms);
+void hj_result_free(hj_result* res);
+
+/* ---- hash table on device columns (UnchainedHash semantics) -------------- */
+
+/* Builds the unchained table over device keys.  keys: int32[n] in HBM;
+ * valid: validity bitmap in HBM (bit i%32 of word i/32 set = row i non-NULL) or
+ * NULL when every row is valid.  NULL rows are not inserted.  dir_bits < 0 sizes
+ * the directory as UnchainedHash does: next_pow2(#inserted), i.e. the same
+ * directory words for the same key multiset. */
+int hj_table_build(hj_context* ctx, const int32_t* keys, const uint32_t* valid, uint64_t n,
+                   int32_t dir_bits, hj_hash_table** out);
+/* Device pointers of the built table: directory (2^dir_bits + 1 words of
+ * (first tuple << 16 | 16-bit Bloom tag)), tuple keys and build row ids in
+ * adjacency-array order. */
+int hj_table_info(const hj_hash_table* t, uint32_t* dir_bits, uint64_t* num_tuples,
+                  const uint64_t** dir, const int32_t** tuple_keys, const uint32_t** tuple_rows);
+/* Probes the table with device keys (NULL rows never match) and writes every
+ * match as (probe row, build row) into caller buffers in HBM.  If more than
+ * `capacity` matches exist nothing is written, *num_matches is set to the
+ * count and HJ_ERR_CAPACITY is returned. */
+int hj_table_probe(hj_context* ctx, const hj_hash_table* t, const int32_t* keys,
+                   const uint32_t* valid, uint64_t n, uint32_t* out_probe_rows,
+                   uint32_t* out_build_rows, uint64_t capacity, uint64_t* num_matches);
+void hj_table_free(hj_hash_table* t);
+
+/* ---- host page writers (Table::to_columnar / ColumnInserter packing) ----- */
+
+/* INT32 column of n rows into pages: valid (one byte per row, 0 = NULL) may be
+ * NULL for "all valid".  With out == NULL only *num_pages is computed. */
+int hj_pages_from_int32(const int32_t* values, const uint8_t* valid, uint64_t n, void* out,
+                        uint64_t capacity_pages, uint64_t* num_pages);
+/* VARCHAR column: string i is bytes[offsets[i] .. offsets[i+1]); valid as above. */
+int hj_pages_from_strings(const uint8_t* bytes, const uint64_t* offsets, const uint8_t* valid,
+                          uint64_t n, void* out, uint64_t capacity_pages, uint64_t* num_pages);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HJ_API_H */

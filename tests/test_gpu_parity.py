@@ -1,0 +1,219 @@
+"""GPU results through the C ABI against the oracle and the reference's
+recorded answers.  Bit-exact: same row count, same multiset of rows (sorted
+rows for small results, sorted 64-bit row fingerprints and their sum for
+large ones); NULLs and string bytes included."""
+from __future__ import annotations
+
+import hashlib
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import cases
+from conftest import canon
+
+pytestmark = pytest.mark.gpu
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+def gpu_out(orc, res):
+    """engine Result -> oracle Output (so the oracle's reader checks it)."""
+    return orc.Output(0, "", res.num_rows, [(c.type, c.pages) for c in res.columns])
+
+
+def assert_same(orc, gpu_res, ref_out, what=""):
+    g = orc.summary(gpu_out(orc, gpu_res))
+    r = orc.summary(ref_out)
+    assert g[0] == r[0], f"{what}: num_rows {g[0]} != {r[0]}"
+    assert g[1] == r[1], f"{what}: column rows {g[1]} != {r[1]}"
+    assert g[2] == r[2], f"{what}: checksum differs"
+    assert np.array_equal(g[3], r[3]), f"{what}: row multisets differ"
+
+
+@pytest.fixture(scope="module")
+def unit_cases(hj):
+    return cases.build_cases(hj)
+
+
+def test_unit_cases_match_reference(engine, orc, unit_cases):
+    gold = json.loads((GOLDEN / "unit_cases.json").read_text())
+    for name, (plan, truth, types) in unit_cases.items():
+        res = engine.execute(plan)
+        out = gpu_out(orc, res)
+        assert [c.type for c in res.columns] == types, name
+        rows = canon(orc.canonical_rows(out))
+        assert res.num_rows == gold[name]["num_rows"], name
+        assert rows == canon(gold[name]["rows"]), name
+        if truth is not None:
+            assert rows == canon(truth), name
+
+
+def test_seeded_small_workloads_match_reference_checksums(engine, orc):
+    from hjgb300 import workloads
+    gold = json.loads((GOLDEN / "configs_small.json").read_text())
+    for name, g in gold.items():
+        w = getattr(workloads, name)(scale=g["scale"])
+        res = engine.execute(w.plan)
+        n, counts, cks, _ = orc.summary(gpu_out(orc, res))
+        assert (n, counts, str(cks)) == (g["num_rows"], g["column_rows"], g["checksum"]), name
+
+
+@pytest.mark.parametrize("name,scale", [("c1", 1.0), ("c2", 1 / 16), ("c3", 0.1), ("c2", 0.01)])
+def test_workloads_match_oracle(engine, orc, name, scale):
+    from hjgb300 import workloads
+    w = getattr(workloads, name)(scale=scale)
+    res = engine.execute(w.plan)
+    if w.expected_rows >= 0:
+        assert res.num_rows == w.expected_rows
+    assert_same(orc, res, orc.run(orc.port(), w.plan), f"{name}@{scale}")
+
+
+def test_c2_full_size_properties(engine, orc):
+    """16M x 256M (pre-filtered to ~25.6M): exact row count from the key
+    histograms, every column the same length, and the oracle's checksum."""
+    from hjgb300 import workloads
+    w = workloads.c2(1.0)
+    res = engine.execute(w.plan)
+    assert res.num_rows == w.expected_rows
+    out = gpu_out(orc, res)
+    n, counts, cks, fp = orc.summary(out)
+    assert n == w.expected_rows and all(c == n for c in counts)
+    r = orc.summary(orc.run(orc.port(), w.plan))
+    assert (n, counts, cks) == r[:3]
+    assert np.array_equal(fp, r[3])
+
+
+def test_results_independent_of_tunables(engine, orc):
+    from hjgb300 import workloads
+    w = workloads.c2(0.004)
+    want = orc.summary(orc.run(orc.port(), w.plan))
+    for opt in ({"probe_group": 1}, {"probe_group": 4}, {"probe_group": 32}, {"light_max": 1},
+                {"light_max": 4}, {"dir_bits": 8}, {"dir_bits": 20}, {"radix_bits": 0}, {"radix_bits": 6}):
+        saved = {k: engine.get_option(k) for k in opt}
+        try:
+            for k, v in opt.items():
+                engine.set_option(k, v)
+            got = orc.summary(gpu_out(orc, engine.execute(w.plan)))
+        finally:
+            for k, v in saved.items():
+                engine.set_option(k, v)
+        assert got[:3] == want[:3], opt
+        assert np.array_equal(got[3], want[3]), opt
+
+
+def test_resident_tables_give_the_same_result(engine, orc, hj):
+    from hjgb300 import workloads
+    w = workloads.c2(0.01)
+    host = engine.execute(w.plan)
+    res_plan = hj.Plan(w.plan.nodes, [engine.upload(t) for t in w.plan.inputs], w.plan.root)
+    try:
+        a = engine.execute(res_plan)
+        b = engine.execute(res_plan)
+    finally:
+        for t in res_plan.inputs:
+            engine.release(t)
+    sh = orc.summary(gpu_out(orc, host))
+    for r in (a, b):
+        s = orc.summary(gpu_out(orc, r))
+        assert s[:3] == sh[:3] and np.array_equal(s[3], sh[3])
+
+
+def test_error_classes(engine, hj):
+    p = hj.Plan()
+    t = cases.table(hj, [["a"], ["b"]], [cases.V])
+    p.new_input(t)
+    p.new_input(t)
+    p.new_scan_node(0, [(0, cases.V)])
+    p.new_scan_node(1, [(0, cases.V)])
+    p.root = p.new_join_node(True, 0, 1, 0, 0, [(0, cases.V)])
+    with pytest.raises(hj.HjError) as e:
+        engine.execute(p)
+    assert e.value.status == hj.HJ_ERR_RUNTIME and "int32" in str(e.value)
+    p = hj.Plan()
+    for _ in range(1025):
+        p.new_input(cases.table(hj, [[1, "x"]], [cases.I, cases.V]))
+    p.new_scan_node(1024, [(1, cases.V)])
+    p.root = 0
+    with pytest.raises(hj.HjError) as e:
+        engine.execute(p)
+    assert e.value.status == hj.HJ_ERR_OUT_OF_RANGE and "table" in str(e.value)
+    # the context stays usable after an error
+    plan, truth, _ = cases.build_cases(hj)["simple_join"]
+    assert engine.execute(plan).num_rows == 3
+
+
+# ---------------------------------------------------------- hash-table C ABI --
+
+class _Dev:
+    """Zero-copy view of device memory for torch (CUDA array interface)."""
+
+    def __init__(self, ptr, n, typestr):
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": typestr, "data": (ptr, False),
+                                         "version": 3}
+
+
+def _kat_keys(spec):
+    import importlib.util
+    s = importlib.util.spec_from_file_location("make_golden", GOLDEN / "make_golden.py")
+    m = importlib.util.module_from_spec(s)
+    s.loader.exec_module(m)
+    return m.kat_keys(spec)
+
+
+def test_table_directory_is_unchained_hash_directory(engine, hj):
+    """hj_table_build gives the reference UnchainedHash's directory words."""
+    import ctypes as C
+    import torch
+    L = hj.lib()
+    kat = json.loads((GOLDEN / "unchained_kat.json").read_text())
+    for name, e in kat.items():
+        keys = torch.from_numpy(_kat_keys(e["spec"])).cuda()
+        t = C.c_void_p()
+        assert L.hj_table_build(engine.handle, keys.data_ptr(), None, keys.numel(), -1, C.byref(t)) == 0
+        try:
+            bits, nt, d = C.c_uint32(), C.c_uint64(), C.c_void_p()
+            L.hj_table_info(t, C.byref(bits), C.byref(nt), C.byref(d), None, None)
+            assert nt.value == keys.numel()
+            n = (1 << bits.value) + 1
+            assert n == e["dir_size"], name
+            dev = torch.as_tensor(_Dev(d.value, n, "<u8"), device="cuda").cpu().numpy().astype("<u8")
+            if "dir" in e:
+                assert [int(x) for x in dev] == e["dir"], name
+            assert hashlib.sha256(dev.tobytes()).hexdigest() == e["sha256"], name
+        finally:
+            L.hj_table_free(t)
+
+
+def test_table_probe_pairs(engine, hj, orc):
+    import ctypes as C
+    import torch
+    L = hj.lib()
+    r = np.random.default_rng(9)
+    build = (r.zipf(1.2, 200_000) % 50_000).astype(np.int32)
+    build[:3] = [2**31 - 1, -(2**31), -7]
+    probe = r.integers(-100, 60_000, 300_000).astype(np.int32)
+    valid = (r.random(probe.size) > 0.1)
+    bits = np.packbits(valid.astype(np.uint8), bitorder="little")
+    bits = np.pad(bits, (0, (-bits.size) % 4)).view(np.uint32)
+    want = orc.unchained_counts(build, probe) * valid
+    kb, kp = torch.from_numpy(build).cuda(), torch.from_numpy(probe).cuda()
+    vb = torch.from_numpy(bits.copy()).cuda()
+    t = C.c_void_p()
+    assert L.hj_table_build(engine.handle, kb.data_ptr(), None, kb.numel(), -1, C.byref(t)) == 0
+    try:
+        nm = C.c_uint64()
+        rc = L.hj_table_probe(engine.handle, t, kp.data_ptr(), vb.data_ptr(), kp.numel(), None, None, 0,
+                              C.byref(nm))
+        assert rc == hj.HJ_ERR_CAPACITY and nm.value == int(want.sum())
+        op = torch.empty(nm.value, dtype=torch.int32, device="cuda")
+        ob = torch.empty(nm.value, dtype=torch.int32, device="cuda")
+        assert L.hj_table_probe(engine.handle, t, kp.data_ptr(), vb.data_ptr(), kp.numel(), op.data_ptr(),
+                                ob.data_ptr(), nm.value, C.byref(nm)) == 0
+        pr, br = op.cpu().numpy(), ob.cpu().numpy()
+        assert np.array_equal(probe[pr], build[br])          # every pair is a match
+        assert np.array_equal(np.bincount(pr, minlength=probe.size), want)  # and all are there
+        assert np.unique(pr.astype(np.int64) << 32 | br).size == pr.size   # no duplicates
+    finally:
+        L.hj_table_free(t)
