@@ -313,8 +313,11 @@ void build_table(const KeyCol& kc, int dir_bits, int radix_bits, Table& t, uint6
                  cudaStream_t st) {
     t = Table{};
     const uint32_t b_upper = dir_bits >= 0 ? uint32_t(dir_bits) : ceil_log2(std::max<uint64_t>(kc.n, 1));
-    uint32_t       R       = radix_bits >= 0 ? uint32_t(radix_bits)
-                                             : (b_upper > kLocalBits ? b_upper - kLocalBits : 0);
+    // partition fan-out: the requested one, raised to what keeps a partition's
+    // buckets within one shared-memory histogram (2^13) and capped at b
+    const uint32_t R_min   = b_upper > kLocalBits ? b_upper - kLocalBits : 0;
+    uint32_t       R       = radix_bits >= 0 ? std::max<uint32_t>(uint32_t(radix_bits), R_min) : R_min;
+    R                      = std::min(R, b_upper);
     if (R > kMaxRadix) throw Error(HJ_ERR_INVALID, "build side too large for the radix partition");
 
     unsigned long long* d_nvalid = dalloc_n<unsigned long long>(1, st);
