@@ -32,8 +32,9 @@ EXPORTS = [
     "hj_execute", "hj_result_shape", "hj_result_column", "hj_result_copy_pages",
     "hj_result_copy_contiguous", "hj_result_stats", "hj_result_phase_ms", "hj_result_free",
     "hj_table_build", "hj_table_info", "hj_table_probe", "hj_table_free",
-    "hj_pages_from_int32", "hj_pages_from_strings",
+    "hj_pages_from_int32", "hj_pages_from_strings", "hj_table_probe_noalloc",
 ]
+NOALLOC_MAX_PROBE_ROWS = 65536  # HJ_NOALLOC_MAX_PROBE_ROWS
 
 
 class HjError(RuntimeError):
@@ -107,6 +108,7 @@ def lib() -> C.CDLL:
     L.hj_table_info.argtypes = [vp, P(u32), P(u64), P(vp), P(vp), P(vp)]
     L.hj_table_probe.argtypes = [vp, vp, vp, vp, u64, vp, vp, u64, P(u64)]
     L.hj_table_free.argtypes = [vp]
+    L.hj_table_probe_noalloc.argtypes = [vp, vp, vp, vp, u64, vp, vp, u64, P(u64)]
     L.hj_pages_from_int32.argtypes = [vp, vp, u64, vp, u64, P(u64)]
     L.hj_pages_from_strings.argtypes = [vp, vp, vp, u64, vp, u64, P(u64)]
     L.hj_context_destroy.restype = None

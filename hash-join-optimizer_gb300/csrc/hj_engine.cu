@@ -621,6 +621,22 @@ int guarded(hj_context* c, F&& f) {
 }  // namespace
 }  // namespace hj
 
+namespace hj {
+
+int          context_device(const hj_context* c) { return c->device; }
+cudaStream_t context_stream(const hj_context* c) { return c->st; }
+ProbeParams  context_probe_params(const hj_context* c) {
+    ProbeParams p;
+    p.light_max = int(c->light_max);
+    p.group     = int(c->probe_group);
+    p.pinned    = c->pinned;
+    return p;
+}
+void         context_set_error(hj_context* c, const char* msg) { c->err = msg; }
+const Table& hash_table_of(const hj_hash_table* t) { return t->t; }
+
+}  // namespace hj
+
 // ===================================================================== C ABI
 
 extern "C" {

@@ -22,6 +22,11 @@ T* dalloc_n(size_t n, cudaStream_t st) {
 // out[i] = sum(in[0..i)), out[n] = total.  out has n + 1 slots.
 void scan_exclusive_u32_to_u64(const uint32_t* in, uint64_t* out, uint64_t n, cudaStream_t st);
 void scan_exclusive_u64(const uint64_t* in, uint64_t* out, uint64_t n, cudaStream_t st);
+// Same as scan_exclusive_u32_to_u64 with caller-provided temporaries of
+// scan_tmp_words(n) words (n <= 4096^2); allocates nothing.
+size_t scan_tmp_words(uint64_t n);
+void   scan_exclusive_u32_to_u64_into(const uint32_t* in, uint64_t* out, uint64_t n, uint64_t* tmp,
+                                      cudaStream_t st);
 
 // ---- page decode (hj_decode.cu) --------------------------------------------
 // Per page: rows it contributes to its column (0xfffe pages: 0, 0xffff: 1),
@@ -90,6 +95,15 @@ void probe_write(const Table& t, const KeyCol& pk, ProbePlan* pp, const RidOut* 
                  cudaStream_t st);
 void probe_free(ProbePlan* pp, cudaStream_t st);
 
+// Count + write in one call with every temporary carved from `scratch`
+// (probe_scratch_bytes(n) bytes, device memory the caller owns); allocates
+// nothing.  Returns HJ_ERR_CAPACITY (writing nothing) when the matches exceed
+// `capacity`; *num_matches is always set.
+size_t probe_scratch_bytes(uint64_t n);
+int    probe_into_scratch(const Table& t, const KeyCol& pk, const ProbeParams& prm, uint8_t* scratch,
+                          size_t scratch_bytes, uint32_t* out_probe, uint32_t* out_build,
+                          uint64_t capacity, uint64_t* num_matches, cudaStream_t st);
+
 // ---- output pages (hj_materialize.cu) --------------------------------------
 // INT32 output column of n rows gathered through rid (nullptr = identity) from a
 // base column; writes ceil(n / 1984) pages.
@@ -103,4 +117,15 @@ uint64_t write_varchar_pages(const uint64_t* refs, const uint8_t* base_pages,
                              uint64_t base_num_pages, const uint32_t* rid, uint64_t n,
                              uint8_t** out_pages, uint64_t* pinned, cudaStream_t st);
 
+}  // namespace hj
+
+// Read-only views of C-ABI objects for code outside hj_engine.cu.
+struct hj_context;
+struct hj_hash_table;
+namespace hj {
+int             context_device(const hj_context* c);
+cudaStream_t    context_stream(const hj_context* c);
+ProbeParams     context_probe_params(const hj_context* c);  // options + pinned readback
+void            context_set_error(hj_context* c, const char* msg);
+const Table&    hash_table_of(const hj_hash_table* t);
 }  // namespace hj

@@ -386,6 +386,107 @@ void probe_write(const Table& t, const KeyCol& pk, ProbePlan* pp, const RidOut* 
     }
 }
 
+namespace {
+
+// Bump carve-out of 256-byte-aligned pieces from a caller-owned buffer.
+struct Carve {
+    uint8_t* p;
+    size_t   used = 0;
+    template <class T>
+    T* take(uint64_t n) {
+        T* r = reinterpret_cast<T*>(p + used);
+        used += (n * sizeof(T) + 255) & ~size_t(255);
+        return r;
+    }
+};
+
+}  // namespace
+
+size_t probe_scratch_bytes(uint64_t n) {
+    const uint64_t tmp = scan_tmp_words(n) + 1;
+    return 14 * ((4 * n + 255) & ~uint64_t(255)) + 4 * ((8 * (n + 1) + 255) & ~uint64_t(255))
+         + ((8 * tmp + 255) & ~uint64_t(255)) + 256;
+}
+
+int probe_into_scratch(const Table& t, const KeyCol& pk, const ProbeParams& prm, uint8_t* scratch,
+                       size_t scratch_bytes, uint32_t* out_probe, uint32_t* out_build, uint64_t capacity,
+                       uint64_t* num_matches, cudaStream_t st) {
+    *num_matches = 0;
+    if (t.n_tuples == 0 || pk.n == 0) return HJ_OK;
+    const uint64_t n = pk.n;
+    if (probe_scratch_bytes(n) > scratch_bytes) throw Error(HJ_ERR_INVALID, "probe scratch too small");
+    Lists     L{};
+    uint64_t *light_off, *unit_off, *big_off, *mixed_off, *tmp;
+    uint32_t *units, *lens;
+    Carve     c{scratch};
+    L.ctr     = c.take<unsigned long long>(8);
+    L.l_row   = c.take<uint32_t>(n);
+    L.l_s     = c.take<uint32_t>(n);
+    L.l_cnt   = c.take<uint32_t>(n);
+    L.l_key   = c.take<int32_t>(n);
+    L.b_row   = c.take<uint32_t>(n);
+    L.b_s     = c.take<uint32_t>(n);
+    L.b_e     = c.take<uint32_t>(n);
+    L.m_row   = c.take<uint32_t>(n);
+    L.m_s     = c.take<uint32_t>(n);
+    L.m_e     = c.take<uint32_t>(n);
+    L.m_cnt   = c.take<uint32_t>(n);
+    L.m_key   = c.take<int32_t>(n);
+    units     = c.take<uint32_t>(n);
+    lens      = c.take<uint32_t>(n);
+    light_off = c.take<uint64_t>(n + 1);
+    unit_off  = c.take<uint64_t>(n + 1);
+    big_off   = c.take<uint64_t>(n + 1);
+    mixed_off = c.take<uint64_t>(n + 1);
+    tmp       = c.take<uint64_t>(scan_tmp_words(n) + 1);
+    // the scratch keeps the previous call's contents: the counters restart at zero
+    HJ_CUDA(cudaMemsetAsync(L.ctr, 0, 8 * sizeof(unsigned long long), st));
+    const ProbeTab T      = tab_of(t);
+    const uint64_t ntiles = (n + kPTile - 1) / kPTile;
+    const int      grid   = int(std::min<uint64_t>(ntiles, uint64_t(kSMs) * 8));
+    k_probe_count<<<grid, kPT, 0, st>>>(T, pk, prm.light_max, L, ntiles);
+    HJ_LAUNCH_CHECK();
+    k_mixed_count<<<kSMs * 2, 512, 0, st>>>(T, L);
+    HJ_LAUNCH_CHECK();
+    uint64_t* h = prm.pinned;
+    HJ_CUDA(cudaMemcpyAsync(h, L.ctr, 6 * sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+    HJ_CUDA(cudaStreamSynchronize(st));
+    const uint64_t n_light = h[0], n_big = h[1], n_mixed = h[2];
+    const uint64_t tot_light = h[3], tot_big = h[4], total = h[3] + h[4] + h[5];
+    *num_matches = total;
+    if (total > capacity) return HJ_ERR_CAPACITY;
+    if (total == 0) return HJ_OK;
+    Outs outs{};
+    outs.n    = 2;
+    outs.o[0] = RidOut{0, nullptr, out_probe};
+    outs.o[1] = RidOut{1, nullptr, out_build};
+    if (n_light) {
+        scan_exclusive_u32_to_u64_into(L.l_cnt, light_off, n_light, tmp, st);
+        const int g = int(std::min<uint64_t>(div_up(n_light, 256), uint64_t(kSMs) * 16));
+        switch (prm.group) {
+        case 1: k_write_light<1><<<g, 256, 0, st>>>(T, L, n_light, light_off, outs); break;
+        case 4: k_write_light<4><<<g, 256, 0, st>>>(T, L, n_light, light_off, outs); break;
+        case 32: k_write_light<32><<<g, 256, 0, st>>>(T, L, n_light, light_off, outs); break;
+        default: k_write_light<8><<<g, 256, 0, st>>>(T, L, n_light, light_off, outs); break;
+        }
+        HJ_LAUNCH_CHECK();
+    }
+    if (n_big) {
+        k_big_units<<<div_up(n_big, 256), 256, 0, st>>>(L.b_s, L.b_e, n_big, units, lens);
+        HJ_LAUNCH_CHECK();
+        scan_exclusive_u32_to_u64_into(units, unit_off, n_big, tmp, st);
+        scan_exclusive_u32_to_u64_into(lens, big_off, n_big, tmp, st);
+        k_write_big<<<kSMs * 4, 256, 0, st>>>(T, L, n_big, unit_off, big_off, tot_light, outs);
+        HJ_LAUNCH_CHECK();
+    }
+    if (n_mixed) {
+        scan_exclusive_u32_to_u64_into(L.m_cnt, mixed_off, n_mixed, tmp, st);
+        k_write_mixed<<<kSMs * 2, 512, 0, st>>>(T, L, mixed_off, tot_light + tot_big, outs);
+        HJ_LAUNCH_CHECK();
+    }
+    return HJ_OK;
+}
+
 void probe_free(ProbePlan* pp, cudaStream_t st) {
     if (!pp) return;
     Lists& L = pp->ls;

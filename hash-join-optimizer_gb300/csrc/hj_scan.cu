@@ -82,4 +82,32 @@ void scan_exclusive_u64(const uint64_t* in, uint64_t* out, uint64_t n, cudaStrea
     scan_impl<uint64_t>(in, out, n, st);
 }
 
+size_t scan_tmp_words(uint64_t n) {
+    const uint64_t blocks = (n + kScanTile - 1) / kScanTile;
+    return blocks <= 1 ? 0 : size_t(2 * blocks + 1);
+}
+
+void scan_exclusive_u32_to_u64_into(const uint32_t* in, uint64_t* out, uint64_t n, uint64_t* tmp,
+                                    cudaStream_t st) {
+    if (n == 0) {
+        HJ_CUDA(cudaMemsetAsync(out, 0, sizeof(uint64_t), st));
+        return;
+    }
+    const uint64_t blocks = (n + kScanTile - 1) / kScanTile;
+    if (blocks == 1) {
+        k_scan_apply<uint32_t><<<1, kScanThreads, 0, st>>>(in, out, n, nullptr);
+        HJ_LAUNCH_CHECK();
+        return;
+    }
+    if (blocks > uint64_t(kScanTile)) throw Error(HJ_ERR_INVALID, "scan too large for a two-level scan");
+    uint64_t* sums = tmp;
+    uint64_t* offs = tmp + blocks;
+    k_block_sums<uint32_t><<<unsigned(blocks), kScanThreads, 0, st>>>(in, n, sums);
+    HJ_LAUNCH_CHECK();
+    k_scan_apply<uint64_t><<<1, kScanThreads, 0, st>>>(sums, offs, blocks, nullptr);
+    HJ_LAUNCH_CHECK();
+    k_scan_apply<uint32_t><<<unsigned(blocks), kScanThreads, 0, st>>>(in, out, n, offs);
+    HJ_LAUNCH_CHECK();
+}
+
 }  // namespace hj

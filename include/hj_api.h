@@ -183,6 +183,25 @@ int hj_table_probe(hj_context* ctx, const hj_hash_table* t, const int32_t* keys,
                    uint32_t* out_build_rows, uint64_t capacity, uint64_t* num_matches);
 void hj_table_free(hj_hash_table* t);
 
+/* ---- allocation-free probe -------------------------------------------------
+ * No counterpart in the reference.  Same matches as hj_table_probe, for callers
+ * that cannot allocate device memory during the call: engines that hand all
+ * device memory to their own sub-allocator under a fixed budget, embedders
+ * whose CUDA memory pool must not grow after start-up, and latency-critical
+ * paths that cannot afford an allocation.  Every temporary comes from one array of
+ * HJ_NOALLOC_SCRATCH_BYTES inside the library image, which each GPU that loads
+ * the library holds until the process exits; the call itself allocates
+ * nothing.  At most HJ_NOALLOC_MAX_PROBE_ROWS probe rows per call (more:
+ * HJ_ERR_INVALID with a message naming the limit).  The first call on a device
+ * looks up the array's device address and should come before any stream
+ * capture.  All calls share the array: calls whose GPU work overlaps race, so
+ * the caller serialises them. */
+#define HJ_NOALLOC_MAX_PROBE_ROWS 65536u
+#define HJ_NOALLOC_SCRATCH_BYTES (6u << 20)
+int hj_table_probe_noalloc(hj_context* ctx, const hj_hash_table* t, const int32_t* keys,
+                           const uint32_t* valid, uint64_t n, uint32_t* out_probe_rows,
+                           uint32_t* out_build_rows, uint64_t capacity, uint64_t* num_matches);
+
 /* ---- host page writers (Table::to_columnar / ColumnInserter packing) ----- */
 
 /* INT32 column of n rows into pages: valid (one byte per row, 0 = NULL) may be
