@@ -48,10 +48,7 @@ struct Geo {
 
 __device__ __forceinline__ bool load_key(const KeyCol& kc, uint64_t i, int32_t& key) {
     if (i >= kc.n) return false;
-    const uint64_t r = kc.rid ? uint64_t(__ldg(kc.rid + i)) : i;
-    if (!bit_valid(kc.valid, r)) return false;
-    key = __ldg(kc.vals + r);
-    return true;
+    return int_get(kc.col, kc.rid ? uint64_t(__ldg(kc.rid + i)) : i, key);
 }
 
 // 1. Partition histogram + count of valid keys.
@@ -310,9 +307,10 @@ int grid_for(uint64_t work, int threads, int per_sm = 4) {
 }  // namespace
 
 void build_table(const KeyCol& kc, int dir_bits, int radix_bits, Table& t, uint64_t* scratch_host,
-                 cudaStream_t st) {
+                 cudaStream_t st, int64_t n_valid) {
     t = Table{};
-    const uint32_t b_upper = dir_bits >= 0 ? uint32_t(dir_bits) : ceil_log2(std::max<uint64_t>(kc.n, 1));
+    const uint64_t n_upper = n_valid >= 0 ? uint64_t(n_valid) : kc.n;
+    const uint32_t b_upper = dir_bits >= 0 ? uint32_t(dir_bits) : ceil_log2(std::max<uint64_t>(n_upper, 1));
     // partition fan-out: the requested one, raised to what keeps a partition's
     // buckets within one shared-memory histogram (2^13) and capped at b
     const uint32_t R_min   = b_upper > kLocalBits ? b_upper - kLocalBits : 0;
@@ -333,11 +331,13 @@ void build_table(const KeyCol& kc, int dir_bits, int radix_bits, Table& t, uint6
                                          int(smem)));
         k_part_hist<<<grid_for(kc.n, kThreads), kThreads, smem, st>>>(kc, r, part_cnt, d_nvalid);
         HJ_LAUNCH_CHECK();
-        HJ_CUDA(cudaMemcpyAsync(scratch_host, d_nvalid, sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
-        HJ_CUDA(cudaStreamSynchronize(st));
+        if (n_valid < 0) {
+            HJ_CUDA(cudaMemcpyAsync(scratch_host, d_nvalid, sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+            HJ_CUDA(cudaStreamSynchronize(st));
+        }
     };
     run_hist(R);
-    const uint64_t nv = scratch_host[0];
+    const uint64_t nv = n_valid >= 0 ? uint64_t(n_valid) : scratch_host[0];
     if (nv == 0) {  // UnchainedHash with no tuples: no directory, every probe misses
         dfree(part_cnt, st);
         dfree(d_nvalid, st);

@@ -68,6 +68,63 @@ __device__ __forceinline__ uint16_t ld16(const uint8_t* p) {
     return uint16_t(p[0]) | uint16_t(uint16_t(p[1]) << 8);
 }
 
+// An INT32 base column on the device, in one of three forms:
+//  * direct: the raw input pages, every page but the last dense with 1984 rows
+//    (the reference's column_t "direct" mode, include/column_t.h:46-66): row r
+//    is int32 number r % 1984 after the 4-byte header of page r / 1984;
+//  * plain:  int32 values, NULLs marked in an optional validity bitmap;
+//  * tagged: one value_t per row (tag 01 + value, 0 = NULL), so a random
+//    gather fetches value and validity with one load.
+struct IntCol {
+    const uint8_t*  pages  = nullptr;
+    const int32_t*  plain  = nullptr;
+    const uint32_t* valid  = nullptr;  // with `plain` only
+    const uint64_t* tagged = nullptr;
+};
+
+__device__ __forceinline__ bool int_get(const IntCol& c, uint64_t r, int32_t& v) {
+    if (c.tagged) {
+        const uint64_t t = __ldg(c.tagged + r);
+        v                = int32_t(uint32_t(t));
+        return (t >> 62) == 1;
+    }
+    if (c.plain) {
+        v = __ldg(c.plain + r);
+        return bit_valid(c.valid, r);
+    }
+    const uint64_t p = r / uint64_t(kDenseRows);
+    v = __ldg(reinterpret_cast<const int32_t*>(c.pages + p * kPage + 4) + (r - p * uint64_t(kDenseRows)));
+    return true;
+}
+
+// A VARCHAR base column is decoded to one 64-bit locator per row: 0 = NULL;
+// otherwise bit 63 set, bit 62 = long string (0xffff page + 0xfffe pages),
+// bits 40..61 = byte length (saturated at 2^22 - 1 for long strings, whose
+// length is then re-read from their pages), bits 0..39 = byte offset of the
+// string (normal) or of its 0xffff page (long) in the column's page buffer.
+constexpr uint64_t kLocValid   = 1ull << 63;
+constexpr uint64_t kLocLong    = 1ull << 62;
+constexpr uint64_t kLocLenMax  = (1ull << 22) - 1;
+
+__host__ __device__ __forceinline__ uint64_t make_loc(uint64_t off, uint64_t len, bool is_long) {
+    return kLocValid | (is_long ? kLocLong : 0) | ((len < kLocLenMax ? len : kLocLenMax) << 40)
+         | (off & ((1ull << 40) - 1));
+}
+__host__ __device__ __forceinline__ uint64_t loc_off(uint64_t loc) { return loc & ((1ull << 40) - 1); }
+__host__ __device__ __forceinline__ uint64_t loc_len_field(uint64_t loc) { return (loc >> 40) & kLocLenMax; }
+
+// Byte length of a long string starting at the 0xffff page `pg` (its page and
+// the 0xfffe pages after it).
+__device__ __forceinline__ uint32_t long_len(const uint8_t* base, uint64_t pg, uint64_t npages) {
+    uint32_t len = *reinterpret_cast<const uint16_t*>(base + pg * kPage + 2);
+    for (uint64_t q = pg + 1; q < npages; ++q) {
+        const uint8_t* nx = base + q * kPage;
+        if (*reinterpret_cast<const uint16_t*>(nx) != 0xfffe) break;
+        len += *reinterpret_cast<const uint16_t*>(nx + 2);
+    }
+    return len;
+}
+
 inline unsigned div_up(uint64_t a, uint64_t b) { return unsigned((a + b - 1) / b); }
 
 }  // namespace hj

@@ -142,15 +142,46 @@ struct DevColumn {
     int32_t  type      = HJ_INT32;
     uint64_t num_pages = 0;
     Buf      pages;  // raw pages, contiguous
+    // page statistics, read from the page headers on the host at upload
+    uint64_t rows      = 0;      // rows the reference's copy_scan yields
+    uint64_t non_null  = 0;
+    bool     dense1984 = false;  // INT32, no NULLs, every page but the last 1984 rows
+    int64_t  strref_bad_page = -1;  // first page index > 2^18-1 that carries strings
     // decoded form (per execute call)
-    uint64_t rows     = 0;
-    uint64_t non_null = 0;
-    Buf      vals;   // INT32 values
-    Buf      valid;  // validity bitmap (nullptr: no NULLs)
-    Buf      refs;   // VARCHAR value_t
-    bool     decoded  = false;
-    bool     page_overflow = false;  // a page index > 2^18-1 carries strings
+    bool decoded = false;
+    Buf  plain;   // INT32 without NULLs on irregular pages
+    Buf  tagged;  // INT32 with NULLs: value_t per row
+    Buf  locs;    // VARCHAR: locator per row
+
+    IntCol icol() const {
+        IntCol c;
+        if (tagged) c.tagged = tagged->as<uint64_t>();
+        else if (plain) c.plain = plain->as<int32_t>();
+        else if (pages) c.pages = pages->as<uint8_t>();
+        return c;
+    }
 };
+
+// Statistics of one column from its page headers (host side).
+void page_stats(DevColumn& d, const uint16_t* nr, const uint16_t* nn) {
+    d.rows = d.non_null = 0;
+    d.dense1984         = d.type == HJ_INT32;
+    d.strref_bad_page   = -1;
+    for (uint64_t p = 0; p < d.num_pages; ++p) {
+        if (d.type == HJ_INT32) {
+            d.rows += nr[p];
+            d.non_null += nn[p];
+            if (nr[p] != nn[p] || (p + 1 < d.num_pages && nr[p] != kDenseRows)) d.dense1984 = false;
+        } else if (d.type == HJ_VARCHAR) {
+            uint32_t r = nr[p], v = nn[p];
+            if (nr[p] == 0xffff) r = v = 1;
+            else if (nr[p] == 0xfffe) r = v = 0;
+            d.rows += r;
+            d.non_null += v;
+            if (v > 0 && p > StrRef::PAGE_MASK && d.strref_bad_page < 0) d.strref_bad_page = int64_t(p);
+        }
+    }
+}
 
 struct DevTable {
     uint64_t               num_rows = 0;
@@ -214,8 +245,10 @@ void ensure_staging(hj_context* c) {
 
 // Copies `n` host pages into the contiguous device buffer `dst`: pages are
 // gathered by the host threads into a pinned slot while the previous slot is
-// in flight.
-void upload_pages(hj_context* c, const void* const* pages, uint64_t n, uint8_t* dst) {
+// in flight.  The threads also read each page's header (num_rows, second
+// field) into nr/nn.
+void upload_pages(hj_context* c, const void* const* pages, uint64_t n, uint8_t* dst, uint16_t* nr,
+                  uint16_t* nn) {
     if (n == 0) return;
     ensure_staging(c);
     const uint64_t per_slot = kSlot / kPage;
@@ -227,7 +260,12 @@ void upload_pages(hj_context* c, const void* const* pages, uint64_t n, uint8_t* 
         const uint64_t per_task = 256;
         c->pool->parallel_for((cnt + per_task - 1) / per_task, [&](size_t t) {
             const uint64_t a = t * per_task, b = std::min(cnt, a + per_task);
-            for (uint64_t i = a; i < b; ++i) std::memcpy(buf + i * kPage, pages[p0 + i], kPage);
+            for (uint64_t i = a; i < b; ++i) {
+                uint8_t* pg = buf + i * kPage;
+                std::memcpy(pg, pages[p0 + i], kPage);
+                std::memcpy(&nr[p0 + i], pg, 2);
+                std::memcpy(&nn[p0 + i], pg + 2, 2);
+            }
         });
         HJ_CUDA(cudaMemcpyAsync(dst + p0 * kPage, buf, cnt * kPage, cudaMemcpyHostToDevice, c->st));
         HJ_CUDA(cudaEventRecord(c->slot_ev[slot], c->st));
@@ -276,81 +314,64 @@ std::shared_ptr<DevTable> upload_table(hj_context* c, const hj_table_desc& t,
     auto dt      = std::make_shared<DevTable>();
     dt->num_rows = t.num_rows;
     dt->cols.resize(t.num_columns);
+    std::vector<uint16_t> nr, nn;
     for (uint32_t i = 0; i < t.num_columns; ++i) {
         DevColumn& d = dt->cols[i];
         d.type       = t.columns[i].type;
         d.num_pages  = t.columns[i].num_pages;
         if (!want.empty() && !want[i]) continue;
         d.pages = make_buf(std::max<uint64_t>(d.num_pages, 1) * kPage, c->st);
-        upload_pages(c, t.columns[i].pages, d.num_pages, d.pages->as<uint8_t>());
+        nr.assign(d.num_pages, 0);
+        nn.assign(d.num_pages, 0);
+        upload_pages(c, t.columns[i].pages, d.num_pages, d.pages->as<uint8_t>(), nr.data(), nn.data());
+        page_stats(d, nr.data(), nn.data());
     }
     return dt;
 }
 
-// Decodes a device column (idempotent within one execute call).
+// Decodes a device column (idempotent within one execute call); no host
+// synchronisation: sizes come from the page statistics.
 void decode_column(hj_context* c, DevColumn& d, uint32_t table_id, uint32_t col_idx) {
     if (d.decoded) return;
     d.decoded = true;
-    d.rows = d.non_null = 0;
-    if (d.type != HJ_INT32 && d.type != HJ_VARCHAR) return;  // the reference skips these types
-    if (d.num_pages == 0) return;
-    if (!d.pages) throw Error(HJ_ERR_INVALID, "column pages were not uploaded");
-    cudaStream_t st  = c->st;
-    const uint64_t np = d.num_pages;
-    uint32_t* rows  = dalloc_n<uint32_t>(np, st);
-    uint32_t* nn    = dalloc_n<uint32_t>(np, st);
-    uint32_t* flags = dalloc_n<uint32_t>(np, st);
-    uint64_t* rs    = dalloc_n<uint64_t>(np + 1, st);
-    uint64_t* nns   = dalloc_n<uint64_t>(np + 1, st);
-    uint64_t* fl    = dalloc_n<uint64_t>(np + 1, st);
-    launch_page_headers(d.pages->as<uint8_t>(), np, d.type, rows, nn, flags, st);
-    scan_exclusive_u32_to_u64(rows, rs, np, st);
-    scan_exclusive_u32_to_u64(nn, nns, np, st);
-    // flags: count pages with NULLs (bit 0) and with overflowing StrRef pages (bit 1)
-    // by scanning them as integers: bit 1 pages add 2^32.
-    HJ_CUDA(cudaMemcpyAsync(c->pinned, rs + np, 8, cudaMemcpyDeviceToHost, st));
-    HJ_CUDA(cudaMemcpyAsync(c->pinned + 1, nns + np, 8, cudaMemcpyDeviceToHost, st));
-    HJ_CUDA(cudaStreamSynchronize(st));
-    d.rows     = c->pinned[0];
-    d.non_null = c->pinned[1];
-    if (d.type == HJ_VARCHAR && np > StrRef::PAGE_MASK + 1) {
-        // any string on a page beyond the 18-bit page field overflows StrRef
-        std::vector<uint32_t> hf(np);
-        HJ_CUDA(cudaMemcpyAsync(hf.data(), flags, np * 4, cudaMemcpyDeviceToHost, st));
-        HJ_CUDA(cudaStreamSynchronize(st));
-        for (uint64_t p = StrRef::PAGE_MASK + 1; p < np; ++p)
-            if (hf[p] & 2u) {
-                for (void* q : {(void*)rows, (void*)nn, (void*)flags, (void*)rs, (void*)nns, (void*)fl})
-                    dfree(q, st);
-                throw Error(HJ_ERR_OUT_OF_RANGE, "StrRef page overflow: " + std::to_string(p) + " > "
-                                                     + std::to_string(StrRef::PAGE_MASK));
-            }
+    if (d.type != HJ_INT32 && d.type != HJ_VARCHAR) {  // the reference's copy_scan skips these types
+        d.rows = d.non_null = 0;
+        return;
     }
     if (d.type == HJ_VARCHAR && d.non_null > 0) {
+        // the StrRef the reference builds for each string must fit its fields
+        // (include/value_t.h:36-47); same exception class and message
         if (table_id > StrRef::TABLE_MASK)
-            throw Error(HJ_ERR_OUT_OF_RANGE, "StrRef table overflow: " + std::to_string(table_id)
-                                                 + " > " + std::to_string(StrRef::TABLE_MASK));
+            throw Error(HJ_ERR_OUT_OF_RANGE, "StrRef table overflow: " + std::to_string(table_id) + " > "
+                                                 + std::to_string(StrRef::TABLE_MASK));
         if (col_idx > StrRef::COLUMN_MASK)
-            throw Error(HJ_ERR_OUT_OF_RANGE, "StrRef column overflow: " + std::to_string(col_idx)
-                                                 + " > " + std::to_string(StrRef::COLUMN_MASK));
+            throw Error(HJ_ERR_OUT_OF_RANGE, "StrRef column overflow: " + std::to_string(col_idx) + " > "
+                                                 + std::to_string(StrRef::COLUMN_MASK));
+        if (d.strref_bad_page >= 0)
+            throw Error(HJ_ERR_OUT_OF_RANGE, "StrRef page overflow: " + std::to_string(d.strref_bad_page)
+                                                 + " > " + std::to_string(StrRef::PAGE_MASK));
     }
-    const uint64_t words = (d.rows + 31) / 32 + 1;
-    if (d.type == HJ_INT32) {
-        d.vals = make_buf(std::max<uint64_t>(d.rows, 1) * 4, st);
-        if (d.non_null != d.rows) {
-            d.valid = make_buf(words * 4, st);
-            HJ_CUDA(cudaMemsetAsync(d.valid->p, 0, words * 4, st));
-        }
-        launch_decode_int32(d.pages->as<uint8_t>(), np, rs, d.vals->as<int32_t>(),
-                            d.valid ? d.valid->as<uint32_t>() : nullptr, st);
+    if (d.num_pages == 0 || d.rows == 0) return;
+    if (!d.pages) throw Error(HJ_ERR_INVALID, "column pages were not uploaded");
+    if (d.type == HJ_INT32 && d.dense1984) return;  // read in place (direct mode)
+    cudaStream_t   st = c->st;
+    const uint64_t np = d.num_pages;
+    uint32_t*      pr = dalloc_n<uint32_t>(np, st);
+    uint64_t*      rs = dalloc_n<uint64_t>(np + 1, st);
+    launch_page_rows(d.pages->as<uint8_t>(), np, d.type, pr, st);
+    scan_exclusive_u32_to_u64(pr, rs, np, st);
+    if (d.type == HJ_INT32 && d.non_null == d.rows) {
+        d.plain = make_buf(d.rows * 4, st);
+        launch_decode_int32_plain(d.pages->as<uint8_t>(), np, rs, d.plain->as<int32_t>(), st);
+    } else if (d.type == HJ_INT32) {
+        d.tagged = make_buf(d.rows * 8, st);
+        launch_decode_int32_tagged(d.pages->as<uint8_t>(), np, rs, d.tagged->as<uint64_t>(), st);
     } else {
-        d.refs  = make_buf(std::max<uint64_t>(d.rows, 1) * 8, st);
-        d.valid = make_buf(words * 4, st);
-        HJ_CUDA(cudaMemsetAsync(d.valid->p, 0, words * 4, st));
-        launch_decode_varchar(d.pages->as<uint8_t>(), np, rs, table_id, col_idx, d.refs->as<uint64_t>(),
-                              d.valid->as<uint32_t>(), st);
+        d.locs = make_buf(d.rows * 8, st);
+        launch_decode_varchar_loc(d.pages->as<uint8_t>(), np, rs, d.locs->as<uint64_t>(), st);
     }
-    for (void* q : {(void*)rows, (void*)nn, (void*)flags, (void*)rs, (void*)nns, (void*)fl}) dfree(q, st);
+    dfree(pr, st);
+    dfree(rs, st);
 }
 
 // ------------------------------------------------------------ intermediates --
@@ -422,8 +443,19 @@ struct Exec {
             in.cols.push_back(ColRef{0, t, col});
         }
         // rows: those of the first output column, as the reference's result
-        // columns count them (column_t::rows_num)
+        // columns count them (column_t::rows_num).  Output columns of one scan
+        // must agree (the reference indexes them with the same row numbers);
+        // INT64/FP64 columns are empty in the reference and are not compared.
         if (n.num_attrs > 0) in.rows = column(t, uint32_t(n.attrs[0].index)).rows;
+        int64_t common = -1;
+        for (uint32_t a = 0; a < n.num_attrs; ++a) {
+            const DevColumn& d = column(t, uint32_t(n.attrs[a].index));
+            if (d.type != HJ_INT32 && d.type != HJ_VARCHAR) continue;
+            if (common >= 0 && uint64_t(common) != d.rows)
+                throw Error(HJ_ERR_INVALID, "columns of input table " + std::to_string(t)
+                                                + " have different row counts");
+            common = int64_t(d.rows);
+        }
         return in;
     }
 
@@ -432,29 +464,31 @@ struct Exec {
         DevColumn& d = column(cr.table, cr.col);
         if (!in.srcs[cr.src].rid) return d.non_null;
         if (d.non_null == 0 || in.rows == 0) return 0;
-        if (d.non_null == d.rows && !d.valid) return in.rows;
-        // count through the row ids on the host (rare path: VARCHAR join keys)
-        std::vector<uint32_t> rid(in.rows), bm((d.rows + 31) / 32 + 1);
+        if (d.non_null == d.rows) return in.rows;
+        // count through the row ids on the host (rare: VARCHAR join keys and
+        // type-mismatched output columns)
+        const Buf&            vec = d.type == HJ_VARCHAR ? d.locs : d.tagged;
+        std::vector<uint32_t> rid(in.rows);
+        std::vector<uint64_t> v(d.rows);
         HJ_CUDA(cudaMemcpyAsync(rid.data(), in.srcs[cr.src].rid->p, in.rows * 4, cudaMemcpyDeviceToHost, c->st));
-        HJ_CUDA(cudaMemcpyAsync(bm.data(), d.valid->p, bm.size() * 4, cudaMemcpyDeviceToHost, c->st));
+        HJ_CUDA(cudaMemcpyAsync(v.data(), vec->p, d.rows * 8, cudaMemcpyDeviceToHost, c->st));
         HJ_CUDA(cudaStreamSynchronize(c->st));
         uint64_t k = 0;
-        for (uint32_t r : rid) k += (bm[r >> 5] >> (r & 31)) & 1u;
+        for (uint32_t r : rid) k += v[r] != 0;
         return k;
     }
 
     KeyCol key_col(const Inter& in, const ColRef& cr) {
         DevColumn& d = column(cr.table, cr.col);
         KeyCol     k{};
-        k.n = in.rows;
-        if (d.type != HJ_INT32) {  // INT64/FP64 key: the reference's key column is empty
+        // the reference loops over the key column's own rows (execute.cpp:78,88)
+        k.n = in.srcs[cr.src].rid ? in.rows : std::min(in.rows, d.rows);
+        if (d.type != HJ_INT32 || d.rows == 0) {  // INT64/FP64 key: the reference's key column is empty
             k.n = 0;
             return k;
         }
-        if (d.rows == 0) k.n = 0;
-        k.vals  = d.vals ? d.vals->as<int32_t>() : nullptr;
-        k.valid = d.valid ? d.valid->as<uint32_t>() : nullptr;
-        k.rid   = in.srcs[cr.src].rid ? in.srcs[cr.src].rid->as<uint32_t>() : nullptr;
+        k.col = d.icol();
+        k.rid = in.srcs[cr.src].rid ? in.srcs[cr.src].rid->as<uint32_t>() : nullptr;
         return k;
     }
 
@@ -499,7 +533,13 @@ struct Exec {
         probe_tuples += pkc.n;
         Table t;
         phase("build");
-        build_table(bkc, int(c->dir_bits), int(c->radix_bits), t, c->pinned, c->st);
+        // valid build keys, when known without a device count: all rows if the
+        // key column has no NULLs, its non-NULL count when read without row ids
+        const DevColumn& bd   = column(bk.table, bk.col);
+        int64_t          hint = -1;
+        if (bkc.n == 0 || bd.non_null == bd.rows) hint = int64_t(bkc.n);
+        else if (!bkc.rid) hint = int64_t(bd.non_null);
+        build_table(bkc, int(c->dir_bits), int(c->radix_bits), t, c->pinned, c->st, hint);
         phase("probe");
         ProbeParams prm;
         prm.light_max = int(c->light_max);
@@ -544,46 +584,62 @@ struct Exec {
 
     void materialize(const Inter& in, const hj_node_desc& root, hj_result* res) {
         phase("materialize");
+        res->cols.assign(root.num_attrs, hj_result::Col{0, 0, nullptr});
+        std::vector<std::pair<uint32_t, VarcharOut>> vout;  // (column, plan)
         for (uint32_t a = 0; a < root.num_attrs; ++a) {
-            const ColRef&   cr = in.cols[a];
-            const int32_t   ty = root.attrs[a].type;
-            DevColumn&      d  = column(cr.table, cr.col);
+            const ColRef&   cr  = in.cols[a];
+            const int32_t   ty  = root.attrs[a].type;
+            DevColumn&      d   = column(cr.table, cr.col);
             const uint32_t* rid = in.srcs[cr.src].rid ? in.srcs[cr.src].rid->as<uint32_t>() : nullptr;
-            hj_result::Col  oc{ty, 0, nullptr};
+            hj_result::Col& oc  = res->cols[a];
+            oc.type             = ty;
             // rows of this output column: the scan column's own count at a scan root
             const uint64_t rows = in.srcs[cr.src].rid ? in.rows : d.rows;
+            if (rows == 0 || (d.type != HJ_INT32 && d.type != HJ_VARCHAR)) continue;
             if (ty == HJ_INT32) {
                 // A StrRef in an INT32 output column leaves the reference's bitmap
-                // undefined (execute.cpp:467-485); it is rejected here.
-                if (d.type == HJ_VARCHAR && non_null_through(in, cr) > 0)
-                    throw Error(HJ_ERR_RUNTIME, "VARCHAR value in an INT32 output column");
-                if ((d.type == HJ_INT32 || d.type == HJ_VARCHAR) && rows > 0) {
-                    oc.num_pages = (rows + kDenseRows - 1) / kDenseRows;
-                    oc.pages     = make_buf(oc.num_pages * kPage, c->st);
-                    launch_write_int32_pages(d.vals ? d.vals->as<int32_t>() : nullptr,
-                                             d.valid ? d.valid->as<uint32_t>() : nullptr, rid, rows,
-                                             oc.pages->as<uint8_t>(), c->st);
+                // undefined (execute.cpp:467-485); it is rejected here.  All-NULL
+                // VARCHAR rows become NULL INT32 rows (their locators read as NULL).
+                IntCol col = d.icol();
+                if (d.type == HJ_VARCHAR) {
+                    if (non_null_through(in, cr) > 0)
+                        throw Error(HJ_ERR_RUNTIME, "VARCHAR value in an INT32 output column");
+                    col        = IntCol{};
+                    col.tagged = d.locs->as<uint64_t>();
                 }
+                oc.num_pages = (rows + kDenseRows - 1) / kDenseRows;
+                oc.pages     = make_buf(oc.num_pages * kPage, c->st);
+                launch_write_int32_pages(col, rid, rows, oc.pages->as<uint8_t>(), c->st);
             } else if (ty == HJ_VARCHAR) {
-                if (d.type == HJ_INT32 && non_null_through(in, cr) > 0)
-                    throw Error(HJ_ERR_RUNTIME, "not string or null");
-                if (d.type == HJ_VARCHAR && rows > 0) {
-                    uint8_t* pages = nullptr;
-                    oc.num_pages   = write_varchar_pages(d.refs->as<uint64_t>(), d.pages->as<uint8_t>(),
-                                                         d.num_pages, rid, rows, &pages, c->pinned, c->st);
-                    oc.pages       = std::make_shared<DevBuf>(static_cast<void*>(pages), c->st);
+                VarcharOut v{};
+                if (d.type == HJ_INT32) {
+                    // the reference throws on a non-NULL INT32 here (execute.cpp:561-563);
+                    // an all-NULL one gives NULL strings (tagged NULL = locator NULL = 0)
+                    if (non_null_through(in, cr) > 0) throw Error(HJ_ERR_RUNTIME, "not string or null");
+                    v.locs = d.tagged->as<uint64_t>();
+                } else {
+                    v.locs       = d.locs->as<uint64_t>();
+                    v.base       = d.pages->as<uint8_t>();
+                    v.base_pages = d.num_pages;
                 }
-                // an INT32 column that is all NULL, declared VARCHAR: all-NULL pages
-                if (d.type == HJ_INT32 && rows > 0) {
-                    Buf zero = make_buf(std::max<uint64_t>(d.rows, 1) * 8, c->st);
-                    HJ_CUDA(cudaMemsetAsync(zero->p, 0, std::max<uint64_t>(d.rows, 1) * 8, c->st));
-                    uint8_t* pages = nullptr;
-                    oc.num_pages   = write_varchar_pages(zero->as<uint64_t>(), nullptr, 0, rid, rows, &pages,
-                                                         c->pinned, c->st);
-                    oc.pages       = std::make_shared<DevBuf>(static_cast<void*>(pages), c->st);
-                }
+                v.rid = rid;
+                v.n   = rows;
+                varchar_plan(v, c->st);
+                vout.emplace_back(a, v);
             }
-            res->cols.push_back(std::move(oc));
+        }
+        if (!vout.empty()) {  // one synchronisation for the page counts of every VARCHAR column
+            for (size_t i = 0; i < vout.size(); ++i)
+                HJ_CUDA(cudaMemcpyAsync(c->pinned + i, vout[i].second.tile_off + vout[i].second.ntiles,
+                                        sizeof(uint64_t), cudaMemcpyDeviceToHost, c->st));
+            HJ_CUDA(cudaStreamSynchronize(c->st));
+            std::vector<uint64_t> pages(c->pinned, c->pinned + vout.size());
+            for (size_t i = 0; i < vout.size(); ++i) {
+                hj_result::Col& oc = res->cols[vout[i].first];
+                oc.num_pages       = pages[i];
+                oc.pages = std::make_shared<DevBuf>(static_cast<void*>(varchar_write(vout[i].second, pages[i], c->st)),
+                                                    c->st);
+            }
         }
         // ColumnarTable::num_rows = rows of the first result column (execute.cpp:437)
         if (root.num_attrs == 0) {
@@ -779,7 +835,7 @@ int hj_execute(hj_context* c, const hj_plan_desc* plan, hj_result** out) {
                 auto dt = std::make_shared<hj::DevTable>(*it->second);
                 for (auto& col : dt->cols) {
                     col.decoded = false;
-                    col.vals = col.valid = col.refs = nullptr;
+                    col.plain = col.tagged = col.locs = nullptr;
                 }
                 ex.tables.push_back(dt);
             } else {
@@ -877,8 +933,11 @@ int hj_table_build(hj_context* c, const int32_t* keys, const uint32_t* valid, ui
     ht->st   = c->st;
     const int rc = hj::guarded(c, [&] {
         if (n > 0xffffffffull) throw hj::Error(HJ_ERR_INVALID, "more than 2^32 build rows");
-        hj::KeyCol kc{keys, valid, nullptr, n};
-        hj::build_table(kc, dir_bits, int(c->radix_bits), ht->t, c->pinned, c->st);
+        hj::IntCol col;
+        col.plain = keys;
+        col.valid = valid;
+        hj::KeyCol kc{col, nullptr, n};
+        hj::build_table(kc, dir_bits, int(c->radix_bits), ht->t, c->pinned, c->st, valid ? -1 : int64_t(n));
         HJ_CUDA(cudaStreamSynchronize(c->st));
     });
     if (rc != HJ_OK) {
@@ -907,7 +966,10 @@ int hj_table_probe(hj_context* c, const hj_hash_table* t, const int32_t* keys, c
     int status = HJ_OK;
     const int rc = hj::guarded(c, [&] {
         if (n > 0xffffffffull) throw hj::Error(HJ_ERR_INVALID, "more than 2^32 probe rows");
-        hj::KeyCol      pk{keys, valid, nullptr, n};
+        hj::IntCol col;
+        col.plain = keys;
+        col.valid = valid;
+        hj::KeyCol      pk{col, nullptr, n};
         hj::ProbeParams prm;
         prm.light_max = int(c->light_max);
         prm.group     = int(c->probe_group);

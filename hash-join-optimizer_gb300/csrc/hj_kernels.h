@@ -6,6 +6,8 @@
 
 #include <cstdint>
 
+#include "hj_common.cuh"
+
 namespace hj {
 
 // Stream-ordered device memory (cudaMallocAsync on a pool that keeps freed
@@ -29,25 +31,21 @@ void   scan_exclusive_u32_to_u64_into(const uint32_t* in, uint64_t* out, uint64_
                                       cudaStream_t st);
 
 // ---- page decode (hj_decode.cu) --------------------------------------------
-// Per page: rows it contributes to its column (0xfffe pages: 0, 0xffff: 1),
-// non-NULL rows, and flags (bit 0: page has NULLs; bit 1: page index exceeds
-// the 18-bit StrRef field and carries strings).
-void launch_page_headers(const uint8_t* pages, uint64_t num_pages, int32_t type,
-                         uint32_t* rows, uint32_t* non_null, uint32_t* flags, cudaStream_t st);
-// INT32 pages -> values + validity bitmap (bitmap pre-zeroed, or nullptr when the
-// column has no NULLs).  row_start: exclusive scan of page rows.
-void launch_decode_int32(const uint8_t* pages, uint64_t num_pages, const uint64_t* row_start,
-                         int32_t* vals, uint32_t* valid, cudaStream_t st);
-// VARCHAR pages -> value_t per row (StrRef(table, column, page, ordinal) or 0 =
-// NULL) + validity bitmap (pre-zeroed).
-void launch_decode_varchar(const uint8_t* pages, uint64_t num_pages, const uint64_t* row_start,
-                           uint32_t table_id, uint32_t column, uint64_t* refs, uint32_t* valid,
-                           cudaStream_t st);
+// rows[p] = rows page p contributes to its column (VARCHAR: 0xffff -> 1, 0xfffe -> 0).
+void launch_page_rows(const uint8_t* pages, uint64_t num_pages, int32_t type, uint32_t* rows,
+                      cudaStream_t st);
+// row_start: exclusive scan of page rows.  INT32 -> value_t per row; INT32
+// without NULLs -> int32 per row; VARCHAR -> locator per row (hj_common.cuh).
+void launch_decode_int32_tagged(const uint8_t* pages, uint64_t num_pages, const uint64_t* row_start,
+                                uint64_t* out, cudaStream_t st);
+void launch_decode_int32_plain(const uint8_t* pages, uint64_t num_pages, const uint64_t* row_start,
+                               int32_t* out, cudaStream_t st);
+void launch_decode_varchar_loc(const uint8_t* pages, uint64_t num_pages, const uint64_t* row_start,
+                               uint64_t* out, cudaStream_t st);
 
 // ---- unchained table build (hj_build.cu) -----------------------------------
 struct KeyCol {
-    const int32_t*  vals;   // values of the base column
-    const uint32_t* valid;  // validity bitmap of the base column or nullptr
+    IntCol          col;    // the base column
     const uint32_t* rid;    // row ids into the base column, or nullptr = identity
     uint64_t        n;      // rows of the (intermediate) column
 };
@@ -62,10 +60,11 @@ struct Table {
 };
 
 // Builds `t` over the valid keys of `kc`.  dir_bits < 0: next_pow2(#valid).
-// radix_bits < 0: automatic.  Allocates t's arrays with dalloc.  Synchronises
-// once (to size the directory).
+// radix_bits < 0: automatic.  Allocates t's arrays with dalloc.  n_valid: the
+// number of valid keys when the caller knows it (>= 0), else the build reads
+// it back from the device (one synchronisation).
 void build_table(const KeyCol& kc, int dir_bits, int radix_bits, Table& t, uint64_t* scratch_host,
-                 cudaStream_t st);
+                 cudaStream_t st, int64_t n_valid = -1);
 void free_table(Table& t, cudaStream_t st);
 
 // ---- probe (hj_probe.cu) ---------------------------------------------------
@@ -107,15 +106,27 @@ int    probe_into_scratch(const Table& t, const KeyCol& pk, const ProbeParams& p
 // ---- output pages (hj_materialize.cu) --------------------------------------
 // INT32 output column of n rows gathered through rid (nullptr = identity) from a
 // base column; writes ceil(n / 1984) pages.
-void launch_write_int32_pages(const int32_t* vals, const uint32_t* valid, const uint32_t* rid,
-                              uint64_t n, uint8_t* out_pages, cudaStream_t st);
+void launch_write_int32_pages(const IntCol& col, const uint32_t* rid, uint64_t n, uint8_t* out_pages,
+                              cudaStream_t st);
 
-// VARCHAR output column: returns the number of pages and writes them into a
-// buffer it allocates (*out_pages, freed by the caller with dfree).
-// `pinned`: >= 2 words of pinned host memory (page-count readback).
-uint64_t write_varchar_pages(const uint64_t* refs, const uint8_t* base_pages,
-                             uint64_t base_num_pages, const uint32_t* rid, uint64_t n,
-                             uint8_t** out_pages, uint64_t* pinned, cudaStream_t st);
+// VARCHAR output columns in two steps, so that several columns share one
+// host synchronisation: plan (gather locators, pack pages, count them into
+// *page_count, a device word) then write (after the caller read the counts).
+struct VarcharOut {
+    const uint64_t* locs;        // locators of the base column
+    const uint8_t*  base;        // its pages
+    uint64_t        base_pages;
+    const uint32_t* rid;         // row ids or nullptr
+    uint64_t        n;           // output rows
+    // filled by varchar_plan
+    uint64_t* ol         = nullptr;  // gathered locators, n
+    uint32_t* tile_pages = nullptr;
+    uint64_t* tile_off   = nullptr;  // ntiles + 1 (last = page count, on the device)
+    uint64_t  ntiles     = 0;
+};
+void     varchar_plan(VarcharOut& v, cudaStream_t st);
+// pages = tile_off[ntiles] as read by the caller; returns the page buffer.
+uint8_t* varchar_write(VarcharOut& v, uint64_t pages, cudaStream_t st);
 
 }  // namespace hj
 

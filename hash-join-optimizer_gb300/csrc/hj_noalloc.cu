@@ -73,7 +73,10 @@ extern "C" int hj_table_probe_noalloc(hj_context* c, const hj_hash_table* t, con
         HJ_CUDA(cudaSetDevice(dev));
         uint8_t*           scratch = hj::scratch_on(dev);
         const cudaStream_t st      = hj::context_stream(c);
-        const hj::KeyCol   pk{keys, valid, nullptr, n};
+        hj::IntCol col;
+        col.plain = keys;
+        col.valid = valid;
+        const hj::KeyCol pk{col, nullptr, n};
         if (hj::probe_scratch_bytes(n) > hj::kNoAllocScratchBytes)
             throw hj::Error(HJ_ERR_INVALID, "probe scratch exceeds the static array");
         const int rc = hj::probe_into_scratch(hj::hash_table_of(t), pk, hj::context_probe_params(c), scratch,

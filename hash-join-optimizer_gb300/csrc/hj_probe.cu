@@ -87,8 +87,7 @@ __global__ void __launch_bounds__(kPT)
             int32_t        key = 0;
             if (j < pk.n) {
                 const uint64_t r = pk.rid ? uint64_t(__ldg(pk.rid + j)) : j;
-                if (bit_valid(pk.valid, r)) {
-                    key                = __ldg(pk.vals + r);
+                if (int_get(pk.col, r, key)) {
                     const uint64_t h   = fib_hash(key);
                     const uint64_t p   = bucket_of(h, T.b);
                     const uint64_t w   = __ldg(T.dir + p);
@@ -243,18 +242,31 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// unit_hit[u] = the big hit that work unit u belongs to.
+__global__ void k_unit_map(const uint64_t* __restrict__ unit_off, uint64_t n_big, uint32_t* __restrict__ unit_hit) {
+    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    for (uint64_t h = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; h < n_big; h += stride)
+        for (uint64_t u = unit_off[h]; u < unit_off[h + 1]; ++u) unit_hit[u] = uint32_t(h);
+}
+
 __global__ void __launch_bounds__(256)
     k_write_big(ProbeTab T, Lists Ls, uint64_t n_big, const uint64_t* __restrict__ unit_off,
-                const uint64_t* __restrict__ big_off, uint64_t base_pos, Outs outs) {
+                const uint32_t* __restrict__ unit_hit, const uint64_t* __restrict__ big_off, uint64_t base_pos,
+                Outs outs) {
     const uint64_t nunits = unit_off[n_big];
     for (uint64_t u = blockIdx.x; u < nunits; u += gridDim.x) {
-        uint64_t lo = 0, hi = n_big;  // largest h with unit_off[h] <= u
-        while (hi - lo > 1) {
-            const uint64_t mid = (lo + hi) >> 1;
-            if (unit_off[mid] <= u) lo = mid;
-            else                    hi = mid;
+        uint64_t h;
+        if (unit_hit) {
+            h = unit_hit[u];
+        } else {  // no map: largest h with unit_off[h] <= u
+            uint64_t lo = 0, hi = n_big;
+            while (hi - lo > 1) {
+                const uint64_t mid = (lo + hi) >> 1;
+                if (unit_off[mid] <= u) lo = mid;
+                else                    hi = mid;
+            }
+            h = lo;
         }
-        const uint64_t h    = lo;
         const uint64_t sub  = u - unit_off[h];
         const uint32_t s0   = Ls.b_s[h] + uint32_t(sub) * kSplit;
         const uint32_t e0   = min(Ls.b_e[h], s0 + kSplit);
@@ -373,9 +385,14 @@ void probe_write(const Table& t, const KeyCol& pk, ProbePlan* pp, const RidOut* 
         HJ_LAUNCH_CHECK();
         scan_exclusive_u32_to_u64(units, unit_off, pp->n_big, st);
         scan_exclusive_u32_to_u64(lens, big_off, pp->n_big, st);
-        k_write_big<<<kSMs * 4, 256, 0, st>>>(T, L, pp->n_big, unit_off, big_off, pp->tot_light, outs);
+        // every big hit has >= 1 unit and units = ceil(len / kSplit) <= 1 + len / kSplit
+        const uint64_t max_units = pp->n_big + pp->tot_big / kSplit + 1;
+        uint32_t*      unit_hit  = dalloc_n<uint32_t>(max_units, st);
+        k_unit_map<<<div_up(pp->n_big, 256), 256, 0, st>>>(unit_off, pp->n_big, unit_hit);
         HJ_LAUNCH_CHECK();
-        for (void* p : {(void*)units, (void*)lens, (void*)unit_off, (void*)big_off}) dfree(p, st);
+        k_write_big<<<kSMs * 8, 256, 0, st>>>(T, L, pp->n_big, unit_off, unit_hit, big_off, pp->tot_light, outs);
+        HJ_LAUNCH_CHECK();
+        for (void* p : {(void*)units, (void*)lens, (void*)unit_off, (void*)big_off, (void*)unit_hit}) dfree(p, st);
     }
     if (pp->n_mixed) {
         uint64_t* off = dalloc_n<uint64_t>(pp->n_mixed + 1, st);
@@ -476,7 +493,16 @@ int probe_into_scratch(const Table& t, const KeyCol& pk, const ProbeParams& prm,
         HJ_LAUNCH_CHECK();
         scan_exclusive_u32_to_u64_into(units, unit_off, n_big, tmp, st);
         scan_exclusive_u32_to_u64_into(lens, big_off, n_big, tmp, st);
-        k_write_big<<<kSMs * 4, 256, 0, st>>>(T, L, n_big, unit_off, big_off, tot_light, outs);
+        // the per-hit unit counts were consumed by the scan above, so their
+        // n-entry array holds the unit map when it fits; otherwise the write
+        // kernel finds each unit's hit by binary search
+        const uint64_t max_units = n_big + h[4] / kSplit + 1;
+        uint32_t*      unit_hit  = max_units <= n ? units : nullptr;
+        if (unit_hit) {
+            k_unit_map<<<div_up(n_big, 256), 256, 0, st>>>(unit_off, n_big, unit_hit);
+            HJ_LAUNCH_CHECK();
+        }
+        k_write_big<<<kSMs * 8, 256, 0, st>>>(T, L, n_big, unit_off, unit_hit, big_off, tot_light, outs);
         HJ_LAUNCH_CHECK();
     }
     if (n_mixed) {
