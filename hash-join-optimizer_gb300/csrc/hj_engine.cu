@@ -20,6 +20,7 @@
 #include <atomic>
 #include <condition_variable>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <functional>
 #include <map>
@@ -325,6 +326,10 @@ std::shared_ptr<DevTable> upload_table(hj_context* c, const hj_table_desc& t,
         nn.assign(d.num_pages, 0);
         upload_pages(c, t.columns[i].pages, d.num_pages, d.pages->as<uint8_t>(), nr.data(), nn.data());
         page_stats(d, nr.data(), nn.data());
+        if (std::getenv("HJ_TRACE_UPLOAD"))
+            std::fprintf(stderr, "[hj upload] column %u type %d pages %llu rows %llu non_null %llu dense1984 %d\n", i,
+                         d.type, (unsigned long long)d.num_pages, (unsigned long long)d.rows,
+                         (unsigned long long)d.non_null, int(d.dense1984));
     }
     return dt;
 }
@@ -453,7 +458,9 @@ struct Exec {
             if (d.type != HJ_INT32 && d.type != HJ_VARCHAR) continue;
             if (common >= 0 && uint64_t(common) != d.rows)
                 throw Error(HJ_ERR_INVALID, "columns of input table " + std::to_string(t)
-                                                + " have different row counts");
+                                                + " have different row counts (" + std::to_string(common)
+                                                + " vs " + std::to_string(d.rows) + " in column "
+                                                + std::to_string(n.attrs[a].index) + ")");
             common = int64_t(d.rows);
         }
         return in;
