@@ -307,10 +307,12 @@ int grid_for(uint64_t work, int threads, int per_sm = 4) {
 }  // namespace
 
 void build_table(const KeyCol& kc, int dir_bits, int radix_bits, Table& t, uint64_t* scratch_host,
-                 cudaStream_t st, int64_t n_valid) {
+                 cudaStream_t st, int64_t n_valid, int dir_cap_bits) {
     t = Table{};
     const uint64_t n_upper = n_valid >= 0 ? uint64_t(n_valid) : kc.n;
-    const uint32_t b_upper = dir_bits >= 0 ? uint32_t(dir_bits) : ceil_log2(std::max<uint64_t>(n_upper, 1));
+    const uint32_t cap     = uint32_t(std::max(0, dir_cap_bits));
+    const uint32_t b_upper = dir_bits >= 0 ? uint32_t(dir_bits)
+                                           : std::min(cap, ceil_log2(std::max<uint64_t>(n_upper, 1)));
     // partition fan-out: the requested one, raised to what keeps a partition's
     // buckets within one shared-memory histogram (2^13) and capped at b
     const uint32_t R_min   = b_upper > kLocalBits ? b_upper - kLocalBits : 0;
@@ -344,7 +346,7 @@ void build_table(const KeyCol& kc, int dir_bits, int radix_bits, Table& t, uint6
         return;
     }
     if (nv > 0xffffffffull) throw Error(HJ_ERR_INVALID, "more than 2^32 build tuples");
-    const uint32_t b = dir_bits >= 0 ? uint32_t(dir_bits) : ceil_log2(nv);
+    const uint32_t b = dir_bits >= 0 ? uint32_t(dir_bits) : std::min(cap, ceil_log2(nv));
     if (R > b) {  // NULLs shrank the directory below the partition fan-out
         dfree(part_cnt, st);
         R = b;

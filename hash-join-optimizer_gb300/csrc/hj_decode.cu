@@ -33,34 +33,40 @@ __global__ void k_page_rows(const uint8_t* __restrict__ pages, uint64_t num_page
     rows[p] = r;
 }
 
-// One block per page (grid-stride over pages): rank of each non-NULL row
-// among the page's non-NULL rows by a block scan of the bitmap bits.
+// One warp per page (grid-stride over pages): 32 rows at a time, each
+// non-NULL row's rank among the page's non-NULL rows comes from a ballot of
+// the bitmap bits, so no block-wide barrier is needed.
 template <class Emit>
-__device__ __forceinline__ void for_rows(const uint8_t* pg, uint32_t nr, uint32_t* sm, Emit&& emit) {
+__device__ __forceinline__ void warp_rows(const uint8_t* pg, uint32_t nr, Emit&& emit) {
+    const unsigned lane      = threadIdx.x & 31;
     const uint8_t* bm        = pg + kPage - (nr + 7) / 8;
     uint32_t       rank_base = 0;
-    for (uint32_t c = 0; c < nr; c += blockDim.x) {
-        const uint32_t i  = c + threadIdx.x;
-        const bool     on = i < nr && ((bm[i >> 3] >> (i & 7)) & 1u);
-        uint32_t       total;
-        const uint32_t rank = rank_base + block_exclusive_scan<uint32_t>(on ? 1u : 0u, sm, &total);
-        if (i < nr) emit(i, on, rank);
-        rank_base += total;
+    for (uint32_t c = 0; c < nr; c += 32) {
+        const uint32_t i   = c + lane;
+        const bool     on  = i < nr && ((bm[i >> 3] >> (i & 7)) & 1u);
+        const unsigned bal = __ballot_sync(0xffffffffu, on);
+        if (i < nr) emit(i, on, rank_base + __popc(bal & ((1u << lane) - 1)));
+        rank_base += __popc(bal);
     }
 }
+
+__device__ __forceinline__ uint64_t global_warp() {
+    return (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+}
+__device__ __forceinline__ uint64_t total_warps() { return (uint64_t(gridDim.x) * blockDim.x) >> 5; }
 
 __global__ void __launch_bounds__(kDecThreads)
     k_decode_int32_tagged(const uint8_t* __restrict__ pages, uint64_t num_pages,
                           const uint64_t* __restrict__ row_start, uint64_t* __restrict__ out) {
-    __shared__ uint32_t sm[33];
-    for (uint64_t p = blockIdx.x; p < num_pages; p += gridDim.x) {
+    for (uint64_t p = global_warp(); p < num_pages; p += total_warps()) {
         const uint8_t* pg   = pages + p * kPage;
         const uint32_t nr   = *reinterpret_cast<const uint16_t*>(pg);
         const int32_t* data = reinterpret_cast<const int32_t*>(pg + 4);
         uint64_t*      o    = out + row_start[p];
-        for_rows(pg, nr, sm, [&](uint32_t i, bool on, uint32_t rank) {
+        warp_rows(pg, nr, [&](uint32_t i, bool on, uint32_t rank) {
             // a well-formed page has rank < num_non_null <= 2047; never read past it
-            o[i] = (on && rank < (kPage - 4) / 4) ? (uint64_t(uint32_t(data[rank])) | value_t::TAG_INT32) : 0ull;
+            o[i] = (on && rank < (kPage - 4) / 4) ? (uint64_t(uint32_t(__ldg(data + rank))) | value_t::TAG_INT32)
+                                                  : 0ull;
         });
     }
 }
@@ -68,32 +74,31 @@ __global__ void __launch_bounds__(kDecThreads)
 __global__ void __launch_bounds__(kDecThreads)
     k_decode_int32_plain(const uint8_t* __restrict__ pages, uint64_t num_pages,
                          const uint64_t* __restrict__ row_start, int32_t* __restrict__ out) {
-    for (uint64_t p = blockIdx.x; p < num_pages; p += gridDim.x) {
+    for (uint64_t p = global_warp(); p < num_pages; p += total_warps()) {
         const uint8_t* pg   = pages + p * kPage;
         const uint32_t nr   = min(uint32_t(*reinterpret_cast<const uint16_t*>(pg)), uint32_t((kPage - 4) / 4));
         const int32_t* data = reinterpret_cast<const int32_t*>(pg + 4);
         int32_t*       o    = out + row_start[p];
-        for (uint32_t i = threadIdx.x; i < nr; i += blockDim.x) o[i] = data[i];
+        for (uint32_t i = threadIdx.x & 31; i < nr; i += 32) o[i] = __ldg(data + i);
     }
 }
 
 __global__ void __launch_bounds__(kDecThreads)
     k_decode_varchar_loc(const uint8_t* __restrict__ pages, uint64_t num_pages,
                          const uint64_t* __restrict__ row_start, uint64_t* __restrict__ out) {
-    __shared__ uint32_t sm[33];
-    for (uint64_t p = blockIdx.x; p < num_pages; p += gridDim.x) {
+    for (uint64_t p = global_warp(); p < num_pages; p += total_warps()) {
         const uint8_t* pg = pages + p * kPage;
         const uint32_t nr = *reinterpret_cast<const uint16_t*>(pg);
         if (nr == 0xfffe) continue;
         if (nr == 0xffff) {
-            if (threadIdx.x == 0) out[row_start[p]] = make_loc(p * kPage, long_len(pages, p, num_pages), true);
+            if ((threadIdx.x & 31) == 0) out[row_start[p]] = make_loc(p * kPage, long_len(pages, p, num_pages), true);
             continue;
         }
         const uint32_t  nn    = *reinterpret_cast<const uint16_t*>(pg + 2);
         const uint16_t* offs  = reinterpret_cast<const uint16_t*>(pg + 4);
         const uint64_t  data0 = p * kPage + 4 + 2 * uint64_t(nn);
         uint64_t*       o     = out + row_start[p];
-        for_rows(pg, nr, sm, [&](uint32_t i, bool on, uint32_t rank) {
+        warp_rows(pg, nr, [&](uint32_t i, bool on, uint32_t rank) {
             uint64_t v = 0;
             if (on && rank < nn && rank < (kPage - 4) / 2) {
                 const uint32_t start = rank == 0 ? 0u : offs[rank - 1];
@@ -104,8 +109,10 @@ __global__ void __launch_bounds__(kDecThreads)
     }
 }
 
+// one warp per page: kDecThreads / 32 pages per block
 unsigned page_grid(uint64_t num_pages) {
-    return unsigned(std::min<uint64_t>(num_pages, uint64_t(kSMs) * 16));
+    const uint64_t blocks = (num_pages + kDecThreads / 32 - 1) / (kDecThreads / 32);
+    return unsigned(std::max<uint64_t>(1, std::min<uint64_t>(blocks, uint64_t(kSMs) * 8)));
 }
 
 }  // namespace

@@ -203,6 +203,7 @@ struct hj_context {
     int64_t             probe_group = 8;
     int64_t             light_max   = 32;
     int64_t             timing      = 0;
+    int64_t             dir_cap_bits = 22;  // automatic directories stay <= 32 MB (L2 resident)
     uint64_t*           pinned      = nullptr;  // small readbacks
     uint8_t*            staging     = nullptr;  // pinned transfer ring
     size_t              staging_bytes = 0;
@@ -546,7 +547,7 @@ struct Exec {
         int64_t          hint = -1;
         if (bkc.n == 0 || bd.non_null == bd.rows) hint = int64_t(bkc.n);
         else if (!bkc.rid) hint = int64_t(bd.non_null);
-        build_table(bkc, int(c->dir_bits), int(c->radix_bits), t, c->pinned, c->st, hint);
+        build_table(bkc, int(c->dir_bits), int(c->radix_bits), t, c->pinned, c->st, hint, int(c->dir_cap_bits));
         phase("probe");
         ProbeParams prm;
         prm.light_max = int(c->light_max);
@@ -768,6 +769,9 @@ int hj_set_option(hj_context* c, const char* name, int64_t v) {
         c->light_max = v;
     } else if (n == "timing") {
         c->timing = v != 0;
+    } else if (n == "dir_cap_bits") {
+        if (v < 0 || v > 32) return HJ_ERR_INVALID;
+        c->dir_cap_bits = v;
     } else {
         c->err = "unknown option " + n;
         return HJ_ERR_INVALID;
@@ -783,6 +787,7 @@ int hj_get_option(const hj_context* c, const char* name, int64_t* v) {
     else if (n == "probe_group") *v = c->probe_group;
     else if (n == "light_max") *v = c->light_max;
     else if (n == "timing") *v = c->timing;
+    else if (n == "dir_cap_bits") *v = c->dir_cap_bits;
     else return HJ_ERR_INVALID;
     return HJ_OK;
 }

@@ -63,8 +63,10 @@ struct Table {
 // radix_bits < 0: automatic.  Allocates t's arrays with dalloc.  n_valid: the
 // number of valid keys when the caller knows it (>= 0), else the build reads
 // it back from the device (one synchronisation).
+// dir_cap_bits bounds the automatic directory size (dir_bits < 0) so the
+// directory stays cache resident; 64 = UnchainedHash sizing exactly.
 void build_table(const KeyCol& kc, int dir_bits, int radix_bits, Table& t, uint64_t* scratch_host,
-                 cudaStream_t st, int64_t n_valid = -1);
+                 cudaStream_t st, int64_t n_valid = -1, int dir_cap_bits = 64);
 void free_table(Table& t, cudaStream_t st);
 
 // ---- probe (hj_probe.cu) ---------------------------------------------------

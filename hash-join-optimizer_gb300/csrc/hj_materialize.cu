@@ -101,13 +101,6 @@ __device__ __forceinline__ uint32_t loc_len(uint64_t loc, const uint8_t* base, u
     return uint32_t(f);
 }
 
-__global__ void k_gather_locs(const uint64_t* __restrict__ locs, const uint32_t* __restrict__ rid, uint64_t n,
-                              uint64_t* __restrict__ ol) {
-    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
-    for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride)
-        ol[i] = __ldg(locs + (rid ? uint64_t(__ldg(rid + i)) : i));
-}
-
 struct PageDesc {
     uint64_t row;    // first row (normal page) or the string's row (long page)
     uint32_t count;  // rows on a normal page; 0 for a long-string page
@@ -182,12 +175,18 @@ __device__ uint32_t pack_tile(const uint64_t* ol, const uint8_t* base, uint64_t 
     return npg;
 }
 
-__global__ void k_pack_count(const uint64_t* __restrict__ ol, const uint8_t* __restrict__ base, uint64_t npages,
+// Gathers the tile's locators through the row ids into `ol` (read back by the
+// later passes in output order) and counts the tile's pages.
+__global__ void k_pack_count(const uint64_t* __restrict__ locs, const uint32_t* __restrict__ rid,
+                             uint64_t* __restrict__ ol, const uint8_t* __restrict__ base, uint64_t npages,
                              uint64_t n, uint64_t ntiles, uint32_t* __restrict__ tile_pages) {
     const uint64_t t = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     if (t >= ntiles) return;
     const uint64_t t0 = t * kStrTile, t1 = (n < t0 + kStrTile ? n : t0 + kStrTile);
-    const uint32_t c  = pack_tile(ol, base, npages, t0, t1, nullptr);
+    for (uint64_t i = t0 + (threadIdx.x & 31); i < t1; i += 32)
+        ol[i] = __ldg(locs + (rid ? uint64_t(__ldg(rid + i)) : i));
+    __syncwarp();
+    const uint32_t c = pack_tile(ol, base, npages, t0, t1, nullptr);
     if ((threadIdx.x & 31) == 0) tile_pages[t] = c;
 }
 
@@ -218,21 +217,29 @@ __device__ __forceinline__ void copy_to_smem(uint8_t* dst, const uint8_t* src, u
     }
 }
 
-__global__ void __launch_bounds__(kMT)
+constexpr int kVW = 4;  // warps (= pages in flight) per block of the VARCHAR writer
+
+// One warp assembles one page in its own 8 KiB of shared memory: no block
+// barriers, so many pages are in flight per SM while string bytes are fetched.
+__global__ void __launch_bounds__(kVW * 32)
     k_write_varchar_pages(const PageDesc* __restrict__ desc, uint64_t ndesc, const uint64_t* __restrict__ ol,
                           const uint8_t* __restrict__ base, uint64_t npages, uint8_t* __restrict__ out) {
-    __shared__ __align__(16) uint8_t img[kPage];
-    __shared__ uint32_t              sm[33];
-    for (uint64_t pi = blockIdx.x; pi < ndesc; pi += gridDim.x) {
+    extern __shared__ uint4 smem_pages[];
+    const unsigned lane = threadIdx.x & 31;
+    uint8_t*       img  = reinterpret_cast<uint8_t*>(smem_pages) + size_t(threadIdx.x >> 5) * kPage;
+    uint4*         w4   = reinterpret_cast<uint4*>(img);
+    const uint64_t gw   = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nw   = (uint64_t(gridDim.x) * blockDim.x) >> 5;
+    for (uint64_t pi = gw; pi < ndesc; pi += nw) {
         const PageDesc d = desc[pi];
-        zero_img(img);
-        __syncthreads();
+        for (uint32_t k = lane; k < kPage / 16; k += 32) w4[k] = make_uint4(0, 0, 0, 0);
+        __syncwarp();
         if (d.count == 0) {  // long-string page `chunk` of the string in row d.row
             const uint64_t loc = ol[d.row];
             const uint32_t L   = loc_len(loc, base, npages);
             const uint32_t beg = d.chunk * kLongChunk;
             const uint32_t len = min(kLongChunk, L - beg);
-            if (threadIdx.x == 0) {
+            if (lane == 0) {
                 *reinterpret_cast<uint16_t*>(img)     = d.chunk == 0 ? 0xffff : 0xfffe;
                 *reinterpret_cast<uint16_t*>(img + 2) = uint16_t(len);
             }
@@ -243,40 +250,41 @@ __global__ void __launch_bounds__(kMT)
                 const uint8_t* pg = base + q * kPage;
                 const uint32_t pl = *reinterpret_cast<const uint16_t*>(pg + 2);
                 const uint32_t lo = max(so, beg), hi = min(so + pl, beg + len);
-                for (uint32_t x = lo + threadIdx.x; x < hi; x += blockDim.x) img[4 + x - beg] = pg[4 + x - so];
+                for (uint32_t x = lo + lane; x < hi; x += 32) img[4 + x - beg] = pg[4 + x - so];
                 so += pl;
             }
         } else {
             const uint32_t data0  = 4 + 2 * d.nn;
             const uint32_t nbytes = (d.count + 7) / 8, bm0 = kPage - nbytes;
             uint32_t       rank0 = 0, byte0 = 0;
-            for (uint32_t c = 0; c < d.count; c += blockDim.x) {
-                const uint32_t i   = c + threadIdx.x;
-                const uint64_t loc = i < d.count ? ol[d.row + i] : 0;
-                const bool     on  = loc != 0;
-                const uint32_t len = on ? uint32_t(loc_len_field(loc)) : 0u;
-                uint32_t       tr, tb;
-                const uint32_t rank = rank0 + block_exclusive_scan<uint32_t>(on ? 1u : 0u, sm, &tr);
-                const uint32_t boff = byte0 + block_exclusive_scan<uint32_t>(len, sm, &tb);
+            for (uint32_t c = 0; c < d.count; c += 32) {
+                const uint32_t i    = c + lane;
+                const uint64_t loc  = i < d.count ? ol[d.row + i] : 0;
+                const bool     on   = loc != 0;
+                const uint32_t len  = on ? uint32_t(loc_len_field(loc)) : 0u;
+                const unsigned bal  = __ballot_sync(0xffffffffu, on);
+                const uint32_t rank = rank0 + __popc(bal & ((1u << lane) - 1));
+                const uint32_t incl = warp_inclusive_scan<uint32_t>(len);
+                const uint32_t boff = byte0 + incl - len;
                 // the packer guarantees both bounds; they are checked so that no
                 // inconsistent descriptor can write outside the page image
                 if (on && rank < d.nn && data0 + boff + len <= bm0) {
                     *reinterpret_cast<uint16_t*>(img + 4 + 2 * rank) = uint16_t(boff + len);
                     copy_to_smem(img + data0 + boff, base + loc_off(loc), len);
                 }
-                const uint32_t b = __ballot_sync(0xffffffffu, on);
-                if ((threadIdx.x & 31) == 0) put_bits(img, bm0, nbytes, c + (threadIdx.x & ~31u), b);
-                rank0 += tr;
-                byte0 += tb;
+                if (lane == 0) put_bits(img, bm0, nbytes, c, bal);
+                rank0 += __popc(bal);
+                byte0 += __shfl_sync(0xffffffffu, incl, 31);
             }
-            if (threadIdx.x == 0) {
+            if (lane == 0) {
                 *reinterpret_cast<uint16_t*>(img)     = uint16_t(d.count);
                 *reinterpret_cast<uint16_t*>(img + 2) = uint16_t(d.nn);
             }
         }
-        __syncthreads();
-        store_page(out + pi * kPage, img);
-        __syncthreads();
+        __syncwarp();
+        uint4* dst = reinterpret_cast<uint4*>(out + pi * kPage);
+        for (uint32_t k = lane; k < kPage / 16; k += 32) dst[k] = w4[k];
+        __syncwarp();
     }
 }
 
@@ -296,14 +304,12 @@ void launch_write_int32_pages(const IntCol& col, const uint32_t* rid, uint64_t n
 
 void varchar_plan(VarcharOut& v, cudaStream_t st) {
     if (v.n == 0) return;
-    v.ol = dalloc_n<uint64_t>(v.n, st);
-    k_gather_locs<<<grid_of(div_up(v.n, 256), 8), 256, 0, st>>>(v.locs, v.rid, v.n, v.ol);
-    HJ_LAUNCH_CHECK();
+    v.ol         = dalloc_n<uint64_t>(v.n, st);
     v.ntiles     = (v.n + kStrTile - 1) / kStrTile;
     v.tile_pages = dalloc_n<uint32_t>(v.ntiles, st);
     v.tile_off   = dalloc_n<uint64_t>(v.ntiles + 1, st);
-    k_pack_count<<<div_up(v.ntiles * 32, 256), 256, 0, st>>>(v.ol, v.base, v.base_pages, v.n, v.ntiles,
-                                                            v.tile_pages);
+    k_pack_count<<<div_up(v.ntiles * 32, 128), 128, 0, st>>>(v.locs, v.rid, v.ol, v.base, v.base_pages, v.n,
+                                                            v.ntiles, v.tile_pages);
     HJ_LAUNCH_CHECK();
     scan_exclusive_u32_to_u64(v.tile_pages, v.tile_off, v.ntiles, st);
 }
@@ -311,11 +317,15 @@ void varchar_plan(VarcharOut& v, cudaStream_t st) {
 uint8_t* varchar_write(VarcharOut& v, uint64_t pages, cudaStream_t st) {
     if (v.n == 0) return nullptr;
     auto* desc = static_cast<PageDesc*>(dalloc(std::max<uint64_t>(pages, 1) * sizeof(PageDesc), st));
-    k_pack_emit<<<div_up(v.ntiles * 32, 256), 256, 0, st>>>(v.ol, v.base, v.base_pages, v.n, v.ntiles, v.tile_off,
+    k_pack_emit<<<div_up(v.ntiles * 32, 128), 128, 0, st>>>(v.ol, v.base, v.base_pages, v.n, v.ntiles, v.tile_off,
                                                            desc);
     HJ_LAUNCH_CHECK();
     auto* out = static_cast<uint8_t*>(dalloc(std::max<uint64_t>(pages, 1) * kPage, st));
-    k_write_varchar_pages<<<grid_of(pages), kMT, 0, st>>>(desc, pages, v.ol, v.base, v.base_pages, out);
+    const int smem = kVW * kPage;
+    HJ_CUDA(cudaFuncSetAttribute(k_write_varchar_pages, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    const unsigned blocks = unsigned(std::max<uint64_t>(1, std::min<uint64_t>((pages + kVW - 1) / kVW,
+                                                                               uint64_t(kSMs) * 7)));
+    k_write_varchar_pages<<<blocks, kVW * 32, smem, st>>>(desc, pages, v.ol, v.base, v.base_pages, out);
     HJ_LAUNCH_CHECK();
     for (void* p : {(void*)desc, (void*)v.ol, (void*)v.tile_pages, (void*)v.tile_off}) dfree(p, st);
     v.ol         = nullptr;

@@ -90,7 +90,8 @@ def test_results_independent_of_tunables(engine, orc):
     w = workloads.c2(0.004)
     want = orc.summary(orc.run(orc.port(), w.plan))
     for opt in ({"probe_group": 1}, {"probe_group": 4}, {"probe_group": 32}, {"light_max": 1},
-                {"light_max": 4}, {"dir_bits": 8}, {"dir_bits": 20}, {"radix_bits": 0}, {"radix_bits": 6}):
+                {"light_max": 4}, {"dir_bits": 8}, {"dir_bits": 20}, {"radix_bits": 0}, {"radix_bits": 6},
+                {"dir_cap_bits": 10}, {"dir_cap_bits": 32}):
         saved = {k: engine.get_option(k) for k in opt}
         try:
             for k, v in opt.items():
