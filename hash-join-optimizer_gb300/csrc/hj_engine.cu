@@ -322,7 +322,9 @@ std::shared_ptr<DevTable> upload_table(hj_context* c, const hj_table_desc& t,
         d.type       = t.columns[i].type;
         d.num_pages  = t.columns[i].num_pages;
         if (!want.empty() && !want[i]) continue;
-        d.pages = make_buf(std::max<uint64_t>(d.num_pages, 1) * kPage, c->st);
+        // 256 bytes of slack: no kernel reads past the pages, but word loads near
+        // the end of the last page never touch another allocation
+        d.pages = make_buf(std::max<uint64_t>(d.num_pages, 1) * kPage + 256, c->st);
         nr.assign(d.num_pages, 0);
         nn.assign(d.num_pages, 0);
         upload_pages(c, t.columns[i].pages, d.num_pages, d.pages->as<uint8_t>(), nr.data(), nn.data());

@@ -199,47 +199,64 @@ __global__ void k_pack_emit(const uint64_t* __restrict__ ol, const uint8_t* __re
     pack_tile(ol, base, npages, t0, t1, desc + tile_off[t]);
 }
 
-// Copies `len` bytes from global `src` (any alignment, inside one 8 KiB page
-// of a 256-byte-aligned buffer) to shared `dst` with aligned 4-byte loads.
-__device__ __forceinline__ void copy_to_smem(uint8_t* dst, const uint8_t* src, uint32_t len) {
+// Copies `len` bytes of a normal string from global `src` (inside an input
+// page) to shared memory at img + dst.  Strings of up to 64 bytes: all covering
+// source words are loaded first (up to 18 independent loads in flight), then
+// aligned destination words are formed with funnel shifts and stored as 32-bit
+// words; the two boundary words, which neighbouring strings share, are stored
+// byte by byte.  Only words that overlap the string are read.
+__device__ __forceinline__ void copy_string(uint8_t* img, uint32_t dst, const uint8_t* src, uint32_t len) {
+    if (len == 0) return;
     const uintptr_t a  = reinterpret_cast<uintptr_t>(src);
-    const uint32_t* w  = reinterpret_cast<const uint32_t*>(a & ~uintptr_t(3));
-    const int       sh = int(a & 3);
-    const uint32_t  nw = (uint32_t(sh) + len + 3) >> 2;
-#pragma unroll 4
-    for (uint32_t k = 0; k < nw; ++k) {
-        const uint32_t x = __ldg(w + k);
+    const uint32_t  sa = uint32_t(a & 3), da = dst & 3;
+    if (len > 64) {  // generic path
+        for (uint32_t k = 0; k < len; ++k) img[dst + k] = src[k];
+        return;
+    }
+    // start one word early when the source is less offset than the destination,
+    // so that destination word j always takes source words j and j + 1
+    const uint32_t  pre = sa < da ? 4u : 0u;
+    const uint32_t* ws  = reinterpret_cast<const uint32_t*>((a & ~uintptr_t(3)) - pre);
+    const uint32_t  so  = sa + pre;          // string start within the loaded words
+    const uint32_t  sh  = 8 * (so - da);     // 0, 8, 16 or 24
+    const uint32_t  nsw = (so + len + 3) / 4;  // loaded words that overlap the string
+    uint32_t        W[19];
 #pragma unroll
-        for (int b = 0; b < 4; ++b) {
-            const int pos = int(4 * k) + b - sh;
-            if (pos >= 0 && pos < int(len)) dst[pos] = uint8_t(x >> (8 * b));
+    for (int k = 0; k < 19; ++k) W[k] = (uint32_t(k) < nsw && (4u * k + 3 >= so)) ? __ldg(ws + k) : 0u;
+    const uint32_t ndw = (da + len + 3) / 4;  // destination words touched
+    uint32_t*      wd  = reinterpret_cast<uint32_t*>(img + (dst & ~3u));
+#pragma unroll
+    for (int j = 0; j < 18; ++j) {
+        if (uint32_t(j) >= ndw) break;
+        const uint32_t D = __funnelshift_r(W[j], W[j + 1], sh);
+        if (j == 0 || uint32_t(j) == ndw - 1) {
+            // boundary word: only the bytes of this string
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+                const int pos = 4 * j + b - int(da);
+                if (pos >= 0 && pos < int(len)) img[(dst & ~3u) + 4 * j + b] = uint8_t(D >> (8 * b));
+            }
+        } else {
+            wd[j] = D;
         }
     }
 }
 
-constexpr int kVW = 4;  // warps (= pages in flight) per block of the VARCHAR writer
-
-// One warp assembles one page in its own 8 KiB of shared memory: no block
-// barriers, so many pages are in flight per SM while string bytes are fetched.
-__global__ void __launch_bounds__(kVW * 32)
+__global__ void __launch_bounds__(kMT)
     k_write_varchar_pages(const PageDesc* __restrict__ desc, uint64_t ndesc, const uint64_t* __restrict__ ol,
                           const uint8_t* __restrict__ base, uint64_t npages, uint8_t* __restrict__ out) {
-    extern __shared__ uint4 smem_pages[];
-    const unsigned lane = threadIdx.x & 31;
-    uint8_t*       img  = reinterpret_cast<uint8_t*>(smem_pages) + size_t(threadIdx.x >> 5) * kPage;
-    uint4*         w4   = reinterpret_cast<uint4*>(img);
-    const uint64_t gw   = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-    const uint64_t nw   = (uint64_t(gridDim.x) * blockDim.x) >> 5;
-    for (uint64_t pi = gw; pi < ndesc; pi += nw) {
+    __shared__ __align__(16) uint8_t img[kPage];
+    __shared__ uint32_t              sm[33];
+    for (uint64_t pi = blockIdx.x; pi < ndesc; pi += gridDim.x) {
         const PageDesc d = desc[pi];
-        for (uint32_t k = lane; k < kPage / 16; k += 32) w4[k] = make_uint4(0, 0, 0, 0);
-        __syncwarp();
+        zero_img(img);
+        __syncthreads();
         if (d.count == 0) {  // long-string page `chunk` of the string in row d.row
             const uint64_t loc = ol[d.row];
             const uint32_t L   = loc_len(loc, base, npages);
             const uint32_t beg = d.chunk * kLongChunk;
             const uint32_t len = min(kLongChunk, L - beg);
-            if (lane == 0) {
+            if (threadIdx.x == 0) {
                 *reinterpret_cast<uint16_t*>(img)     = d.chunk == 0 ? 0xffff : 0xfffe;
                 *reinterpret_cast<uint16_t*>(img + 2) = uint16_t(len);
             }
@@ -250,41 +267,40 @@ __global__ void __launch_bounds__(kVW * 32)
                 const uint8_t* pg = base + q * kPage;
                 const uint32_t pl = *reinterpret_cast<const uint16_t*>(pg + 2);
                 const uint32_t lo = max(so, beg), hi = min(so + pl, beg + len);
-                for (uint32_t x = lo + lane; x < hi; x += 32) img[4 + x - beg] = pg[4 + x - so];
+                for (uint32_t x = lo + threadIdx.x; x < hi; x += blockDim.x) img[4 + x - beg] = pg[4 + x - so];
                 so += pl;
             }
         } else {
             const uint32_t data0  = 4 + 2 * d.nn;
             const uint32_t nbytes = (d.count + 7) / 8, bm0 = kPage - nbytes;
             uint32_t       rank0 = 0, byte0 = 0;
-            for (uint32_t c = 0; c < d.count; c += 32) {
-                const uint32_t i    = c + lane;
-                const uint64_t loc  = i < d.count ? ol[d.row + i] : 0;
-                const bool     on   = loc != 0;
-                const uint32_t len  = on ? uint32_t(loc_len_field(loc)) : 0u;
-                const unsigned bal  = __ballot_sync(0xffffffffu, on);
-                const uint32_t rank = rank0 + __popc(bal & ((1u << lane) - 1));
-                const uint32_t incl = warp_inclusive_scan<uint32_t>(len);
-                const uint32_t boff = byte0 + incl - len;
+            for (uint32_t c = 0; c < d.count; c += blockDim.x) {
+                const uint32_t i   = c + threadIdx.x;
+                const uint64_t loc = i < d.count ? ol[d.row + i] : 0;
+                const bool     on  = loc != 0;
+                const uint32_t len = on ? uint32_t(loc_len_field(loc)) : 0u;
+                uint32_t       tr, tb;
+                const uint32_t rank = rank0 + block_exclusive_scan<uint32_t>(on ? 1u : 0u, sm, &tr);
+                const uint32_t boff = byte0 + block_exclusive_scan<uint32_t>(len, sm, &tb);
                 // the packer guarantees both bounds; they are checked so that no
                 // inconsistent descriptor can write outside the page image
                 if (on && rank < d.nn && data0 + boff + len <= bm0) {
                     *reinterpret_cast<uint16_t*>(img + 4 + 2 * rank) = uint16_t(boff + len);
-                    copy_to_smem(img + data0 + boff, base + loc_off(loc), len);
+                    copy_string(img, data0 + boff, base + loc_off(loc), len);
                 }
-                if (lane == 0) put_bits(img, bm0, nbytes, c, bal);
-                rank0 += __popc(bal);
-                byte0 += __shfl_sync(0xffffffffu, incl, 31);
+                const uint32_t b = __ballot_sync(0xffffffffu, on);
+                if ((threadIdx.x & 31) == 0) put_bits(img, bm0, nbytes, c + (threadIdx.x & ~31u), b);
+                rank0 += tr;
+                byte0 += tb;
             }
-            if (lane == 0) {
+            if (threadIdx.x == 0) {
                 *reinterpret_cast<uint16_t*>(img)     = uint16_t(d.count);
                 *reinterpret_cast<uint16_t*>(img + 2) = uint16_t(d.nn);
             }
         }
-        __syncwarp();
-        uint4* dst = reinterpret_cast<uint4*>(out + pi * kPage);
-        for (uint32_t k = lane; k < kPage / 16; k += 32) dst[k] = w4[k];
-        __syncwarp();
+        __syncthreads();
+        store_page(out + pi * kPage, img);
+        __syncthreads();
     }
 }
 
@@ -321,11 +337,7 @@ uint8_t* varchar_write(VarcharOut& v, uint64_t pages, cudaStream_t st) {
                                                            desc);
     HJ_LAUNCH_CHECK();
     auto* out = static_cast<uint8_t*>(dalloc(std::max<uint64_t>(pages, 1) * kPage, st));
-    const int smem = kVW * kPage;
-    HJ_CUDA(cudaFuncSetAttribute(k_write_varchar_pages, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    const unsigned blocks = unsigned(std::max<uint64_t>(1, std::min<uint64_t>((pages + kVW - 1) / kVW,
-                                                                               uint64_t(kSMs) * 7)));
-    k_write_varchar_pages<<<blocks, kVW * 32, smem, st>>>(desc, pages, v.ol, v.base, v.base_pages, out);
+    k_write_varchar_pages<<<grid_of(pages), kMT, 0, st>>>(desc, pages, v.ol, v.base, v.base_pages, out);
     HJ_LAUNCH_CHECK();
     for (void* p : {(void*)desc, (void*)v.ol, (void*)v.tile_pages, (void*)v.tile_off}) dfree(p, st);
     v.ol         = nullptr;

@@ -277,6 +277,31 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+constexpr uint32_t kMixedWarpMax = 4096;  // mixed buckets up to this size: one warp each
+
+__global__ void __launch_bounds__(256)
+    k_write_mixed_warp(ProbeTab T, Lists Ls, const uint64_t* __restrict__ mixed_off, uint64_t base_pos,
+                       Outs outs) {
+    const uint64_t n    = Ls.ctr[2];
+    const unsigned lane = threadIdx.x & 31;
+    const uint64_t gw   = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nw   = (uint64_t(gridDim.x) * blockDim.x) >> 5;
+    for (uint64_t q = gw; q < n; q += nw) {
+        const uint32_t s = Ls.m_s[q], e = Ls.m_e[q];
+        if (e - s > kMixedWarpMax) continue;
+        const uint32_t prow = Ls.m_row[q];
+        const int32_t  key  = Ls.m_key[q];
+        uint64_t       pos  = base_pos + mixed_off[q];
+        for (uint32_t b = s; b < e; b += 32) {
+            const uint32_t k   = b + lane;
+            const bool     m   = k < e && __ldg(T.keys + k) == key;
+            const unsigned bal = __ballot_sync(0xffffffffu, m);
+            if (m) emit(outs, pos + __popc(bal & ((1u << lane) - 1)), prow, __ldg(T.rows + k));
+            pos += __popc(bal);
+        }
+    }
+}
+
 __global__ void __launch_bounds__(512)
     k_write_mixed(ProbeTab T, Lists Ls, const uint64_t* __restrict__ mixed_off, uint64_t base_pos,
                   Outs outs) {
@@ -284,6 +309,7 @@ __global__ void __launch_bounds__(512)
     const uint64_t n = Ls.ctr[2];
     for (uint64_t q = blockIdx.x; q < n; q += gridDim.x) {
         const uint32_t s = Ls.m_s[q], e = Ls.m_e[q], prow = Ls.m_row[q];
+        if (e - s <= kMixedWarpMax) continue;  // done by k_write_mixed_warp
         const int32_t  key = Ls.m_key[q];
         uint64_t       pos = base_pos + mixed_off[q];
         for (uint32_t b = s; b < e; b += blockDim.x) {
@@ -397,6 +423,8 @@ void probe_write(const Table& t, const KeyCol& pk, ProbePlan* pp, const RidOut* 
     if (pp->n_mixed) {
         uint64_t* off = dalloc_n<uint64_t>(pp->n_mixed + 1, st);
         scan_exclusive_u32_to_u64(L.m_cnt, off, pp->n_mixed, st);
+        k_write_mixed_warp<<<kSMs * 8, 256, 0, st>>>(T, L, off, pp->tot_light + pp->tot_big, outs);
+        HJ_LAUNCH_CHECK();
         k_write_mixed<<<kSMs * 2, 512, 0, st>>>(T, L, off, pp->tot_light + pp->tot_big, outs);
         HJ_LAUNCH_CHECK();
         dfree(off, st);
@@ -507,6 +535,8 @@ int probe_into_scratch(const Table& t, const KeyCol& pk, const ProbeParams& prm,
     }
     if (n_mixed) {
         scan_exclusive_u32_to_u64_into(L.m_cnt, mixed_off, n_mixed, tmp, st);
+        k_write_mixed_warp<<<kSMs * 8, 256, 0, st>>>(T, L, mixed_off, tot_light + tot_big, outs);
+        HJ_LAUNCH_CHECK();
         k_write_mixed<<<kSMs * 2, 512, 0, st>>>(T, L, mixed_off, tot_light + tot_big, outs);
         HJ_LAUNCH_CHECK();
     }
