@@ -63,12 +63,10 @@ __global__ void __launch_bounds__(kThreads)
     const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
     for (uint64_t w0 = uint64_t(blockIdx.x) * blockDim.x + (threadIdx.x & ~31u); w0 < kc.n;
          w0 += stride) {
-        int32_t        key;
-        const bool     ok  = load_key(kc, w0 + (threadIdx.x & 31), key);
-        const unsigned act = __ballot_sync(0xffffffffu, ok);
+        int32_t    key;
+        const bool ok = load_key(kc, w0 + (threadIdx.x & 31), key);
         if (ok) {
-            const uint32_t part = uint32_t(bucket_of(fib_hash(key), R));
-            warp_agg_atomic_add(hist, part, act);
+            atomicAdd(hist + uint32_t(bucket_of(fib_hash(key), R)), 1u);
             ++mine;
         }
     }
@@ -124,9 +122,8 @@ __global__ void __launch_bounds__(kThreads)
         const uint64_t i  = tile0 + uint64_t(k) * kThreads + threadIdx.x;
         const bool     ok = load_key(kc, i, keys[k]);
         parts[k]          = ok ? uint32_t(bucket_of(fib_hash(keys[k]), R)) : 0;
-        const unsigned act = __ballot_sync(0xffffffffu, ok);
         if (ok) {
-            warp_agg_atomic_add(sh, parts[k], act);
+            atomicAdd(sh + parts[k], 1u);
             okmask |= 1u << k;
         }
     }
@@ -136,10 +133,8 @@ __global__ void __launch_bounds__(kThreads)
     __syncthreads();
 #pragma unroll
     for (int k = 0; k < kItems; ++k) {
-        const bool     ok  = (okmask >> k) & 1u;
-        const unsigned act = __ballot_sync(0xffffffffu, ok);
-        if (ok) {
-            const uint32_t pos = warp_agg_atomic_add(sh, parts[k], act);
+        if ((okmask >> k) & 1u) {
+            const uint32_t pos = atomicAdd(sh + parts[k], 1u);
             tkey[pos]          = keys[k];
             trow[pos]          = uint32_t(tile0 + uint64_t(k) * kThreads + threadIdx.x);
         }
@@ -166,6 +161,22 @@ __device__ __forceinline__ bool chunk_range(uint32_t cid, const uint32_t* chunk_
     return true;
 }
 
+// Shared counter addr[slot] += 1 for each active lane, returning the lane's
+// old value.  Lanes of a warp that all carry one slot (a Zipf-heavy key fills
+// whole chunks) need one atomic; otherwise each lane adds on its own.
+__device__ __forceinline__ uint32_t bucket_add(uint32_t* addr, uint32_t slot, unsigned act) {
+    uint32_t     first = 0;
+    const bool   uni   = __match_all_sync(act, slot, reinterpret_cast<int*>(&first)) != 0;
+    const unsigned lane = threadIdx.x & 31;
+    if (uni) {
+        const int leader = __ffs(act) - 1;
+        uint32_t  base   = 0;
+        if (int(lane) == leader) base = atomicAdd(addr + slot, uint32_t(__popc(act)));
+        return __shfl_sync(act, base, leader) + __popc(act & ((1u << lane) - 1));
+    }
+    return atomicAdd(addr + slot, 1u);
+}
+
 // 4. Per-chunk bucket counts and Bloom tags.
 __global__ void __launch_bounds__(kThreads)
     k_bucket_count(Geo g, const uint32_t* __restrict__ chunk_off, const uint32_t* __restrict__ part_off,
@@ -188,8 +199,8 @@ __global__ void __launch_bounds__(kThreads)
         if (ok) {
             const uint64_t h     = fib_hash(tkey[j]);
             const uint32_t local = uint32_t(bucket_of(h, g.b)) & lmask;
-            warp_agg_atomic_add(cnt, local, act);
-            warp_agg_atomic_or(blm, local, bloom_mask(h), act);
+            bucket_add(cnt, local, act);
+            atomicOr(blm + local, bloom_mask(h));
         }
     }
     __syncthreads();
@@ -238,7 +249,7 @@ __global__ void __launch_bounds__(1024)
 }
 
 // 6. Final scatter into bucket order.
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 2)
     k_bucket_scatter(Geo g, const uint32_t* __restrict__ chunk_off, const uint32_t* __restrict__ part_off,
                      const int32_t* __restrict__ tkey, const uint32_t* __restrict__ trow,
                      uint32_t* __restrict__ cursor, int32_t* __restrict__ okey,
@@ -260,7 +271,7 @@ __global__ void __launch_bounds__(kThreads)
         keys[k]           = ok ? tkey[j] : 0;
         loc[k]            = ok ? (uint32_t(bucket_of(fib_hash(keys[k]), g.b)) & lmask) : 0;
         const unsigned act = __ballot_sync(0xffffffffu, ok);
-        if (ok) warp_agg_atomic_add(sh, loc[k], act);
+        if (ok) bucket_add(sh, loc[k], act);
     }
     __syncthreads();
     const uint64_t gb = uint64_t(part) << g.L;
@@ -274,7 +285,7 @@ __global__ void __launch_bounds__(kThreads)
         const bool     ok  = j < e;
         const unsigned act = __ballot_sync(0xffffffffu, ok);
         if (ok) {
-            const uint32_t pos = warp_agg_atomic_add(sh, loc[k], act);
+            const uint32_t pos = bucket_add(sh, loc[k], act);
             okey[pos]          = keys[k];
             orow[pos]          = trow[j];
         }
@@ -291,6 +302,12 @@ __global__ void k_bucket_mixed(uint32_t b, uint64_t n, const uint64_t* __restric
         const uint64_t first = __ldg(dir + p) >> 16;
         if (key[first] != k) atomicOr(mixed + (p >> 5), 1u << (p & 31));
     }
+}
+
+template <class K>
+void prefer_shared(K kernel) {
+    HJ_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 int(cudaSharedmemCarveoutMaxShared)));
 }
 
 uint32_t ceil_log2(uint64_t n) {
@@ -320,6 +337,10 @@ void build_table(const KeyCol& kc, int dir_bits, int radix_bits, Table& t, uint6
     R                      = std::min(R, b_upper);
     if (R > kMaxRadix) throw Error(HJ_ERR_INVALID, "build side too large for the radix partition");
 
+    prefer_shared(k_part_hist);
+    prefer_shared(k_part_scatter);
+    prefer_shared(k_bucket_count);
+    prefer_shared(k_bucket_scatter);
     unsigned long long* d_nvalid = dalloc_n<unsigned long long>(1, st);
     uint32_t*           part_cnt = nullptr;
     auto run_hist = [&](uint32_t r) {

@@ -279,9 +279,13 @@ __global__ void __launch_bounds__(kMT)
                 const uint64_t loc = i < d.count ? ol[d.row + i] : 0;
                 const bool     on  = loc != 0;
                 const uint32_t len = on ? uint32_t(loc_len_field(loc)) : 0u;
-                uint32_t       tr, tb;
-                const uint32_t rank = rank0 + block_exclusive_scan<uint32_t>(on ? 1u : 0u, sm, &tr);
-                const uint32_t boff = byte0 + block_exclusive_scan<uint32_t>(len, sm, &tb);
+                // one scan of (non-NULL count << 16 | bytes): a chunk holds at most
+                // 256 rows and a page at most 8188 bytes, so neither half overflows
+                uint32_t       tot;
+                const uint32_t ex   = block_exclusive_scan<uint32_t>((on ? 0x10000u : 0u) | len, sm, &tot);
+                const uint32_t rank = rank0 + (ex >> 16);
+                const uint32_t boff = byte0 + (ex & 0xffffu);
+                const uint32_t tr = tot >> 16, tb = tot & 0xffffu;
                 // the packer guarantees both bounds; they are checked so that no
                 // inconsistent descriptor can write outside the page image
                 if (on && rank < d.nn && data0 + boff + len <= bm0) {

@@ -79,39 +79,66 @@ __global__ void __launch_bounds__(kPT)
     for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         if (threadIdx.x == 0) s_n = 0;
         __syncthreads();
-#pragma unroll 2
+        // The lookups of a thread's kPI keys are issued phase by phase (keys,
+        // then directory words, then bucket heads) so that up to kPI
+        // independent memory accesses per thread are in flight.
+        int32_t  key[kPI];
+        bool     ok[kPI];
+        uint64_t w[kPI];
+#pragma unroll
+        for (int it = 0; it < kPI; ++it) {
+            const uint64_t j = tile * kPTile + uint64_t(it) * kPT + threadIdx.x;
+            ok[it]           = false;
+            key[it]          = 0;
+            if (j < pk.n) ok[it] = int_get(pk.col, pk.rid ? uint64_t(__ldg(pk.rid + j)) : j, key[it]);
+        }
+#pragma unroll
+        for (int it = 0; it < kPI; ++it) {
+            w[it] = 0;
+            if (ok[it]) {
+                const uint64_t h = fib_hash(key[it]);
+                const uint64_t wd = __ldg(T.dir + bucket_of(h, T.b));
+                const uint32_t m  = bloom_mask(h);
+                w[it]             = (uint32_t(wd) & m) == m ? wd : 0;  // 0: rejected by the Bloom tag
+                ok[it]            = w[it] != 0;
+            }
+        }
+        uint32_t ends[kPI], heads[kPI], mixw[kPI];
+#pragma unroll
+        for (int it = 0; it < kPI; ++it) {
+            ends[it] = heads[it] = mixw[it] = 0;
+            if (ok[it]) {
+                const uint64_t p = bucket_of(fib_hash(key[it]), T.b);
+                ends[it]         = uint32_t(__ldg(T.dir + p + 1) >> 16);
+                heads[it]        = uint32_t(__ldg(T.keys + uint32_t(w[it] >> 16)));
+                mixw[it]         = __ldg(T.mixed + (p >> 5)) >> (p & 31);
+            }
+        }
+#pragma unroll
         for (int it = 0; it < kPI; ++it) {
             const uint64_t j   = tile * kPTile + uint64_t(it) * kPT + threadIdx.x;
             int            cls = 0;  // 0 miss, 1 light, 2 big, 3 mixed
             uint32_t       c = 0, s = 0, e = 0;
-            int32_t        key = 0;
-            if (j < pk.n) {
-                const uint64_t r = pk.rid ? uint64_t(__ldg(pk.rid + j)) : j;
-                if (int_get(pk.col, r, key)) {
-                    const uint64_t h   = fib_hash(key);
-                    const uint64_t p   = bucket_of(h, T.b);
-                    const uint64_t w   = __ldg(T.dir + p);
-                    const uint32_t m   = bloom_mask(h);
-                    if ((uint32_t(w) & m) == m) {
-                        s                = uint32_t(w >> 16);
-                        e                = uint32_t(__ldg(T.dir + p + 1) >> 16);
-                        const uint32_t L = e - s;
-                        const int32_t  k0 = __ldg(T.keys + s);
-                        if (L == 1) {
-                            c   = k0 == key;
-                            cls = c ? 1 : 0;
-                        } else if (!((__ldg(T.mixed + (p >> 5)) >> (p & 31)) & 1u)) {
-                            c   = k0 == key ? L : 0;
-                            cls = c ? (L <= uint32_t(light_max) ? 1 : 2) : 0;
-                        } else if (L <= uint32_t(light_max)) {
-                            for (uint32_t k = s; k < e; ++k) c += __ldg(T.keys + k) == key;
-                            cls = c ? 1 : 0;
-                        } else {
-                            cls = 3;
-                        }
-                    }
+            const int32_t  k = key[it];
+            if (ok[it]) {
+                s                 = uint32_t(w[it] >> 16);
+                e                 = ends[it];
+                const uint32_t L  = e - s;
+                const int32_t  k0 = int32_t(heads[it]);
+                if (L == 1) {
+                    c   = k0 == k;
+                    cls = c ? 1 : 0;
+                } else if (!(mixw[it] & 1u)) {
+                    c   = k0 == k ? L : 0;
+                    cls = c ? (L <= uint32_t(light_max) ? 1 : 2) : 0;
+                } else if (L <= uint32_t(light_max)) {
+                    for (uint32_t q = s; q < e; ++q) c += __ldg(T.keys + q) == k;
+                    cls = c ? 1 : 0;
+                } else {
+                    cls = 3;
                 }
             }
+            const int32_t key = k;
             // light: stage in shared memory
             {
                 const unsigned bal = __ballot_sync(0xffffffffu, cls == 1);
