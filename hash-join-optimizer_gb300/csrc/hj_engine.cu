@@ -204,6 +204,8 @@ struct hj_context {
     int64_t             light_max   = 32;
     int64_t             timing      = 0;
     int64_t             dir_cap_bits = 22;  // automatic directories stay <= 32 MB (L2 resident)
+    bool                ats_capable  = false;  // GPU reads/writes pageable host memory
+    int64_t             host_access  = 1;      // use it for page transfers when capable
     uint64_t*           pinned      = nullptr;  // small readbacks
     uint8_t*            staging     = nullptr;  // pinned transfer ring
     size_t              staging_bytes = 0;
@@ -310,12 +312,45 @@ void download_pages(hj_context* c, const uint8_t* src, uint64_t n, void* const* 
     drain();
 }
 
-// Uploads the listed columns of a host table (others stay empty).
+bool direct_host_access(const hj_context* c) { return c->ats_capable && c->host_access; }
+
+// Uploads the listed columns of a host table (others stay empty).  With
+// direct host access the GPU gathers the pages itself and the page headers
+// come back in one copy for all columns; otherwise host threads stage them.
 std::shared_ptr<DevTable> upload_table(hj_context* c, const hj_table_desc& t,
                                        const std::vector<bool>& want) {
     auto dt      = std::make_shared<DevTable>();
     dt->num_rows = t.num_rows;
     dt->cols.resize(t.num_columns);
+    if (direct_host_access(c)) {
+        std::vector<std::vector<uint16_t>> hnr(t.num_columns), hnn(t.num_columns);
+        std::vector<Buf>                   dhdr(t.num_columns);
+        for (uint32_t i = 0; i < t.num_columns; ++i) {
+            DevColumn& d = dt->cols[i];
+            d.type       = t.columns[i].type;
+            d.num_pages  = t.columns[i].num_pages;
+            if (!want.empty() && !want[i]) continue;
+            d.pages = make_buf(std::max<uint64_t>(d.num_pages, 1) * kPage + 256, c->st);
+            if (d.num_pages == 0) continue;
+            dhdr[i]       = make_buf(d.num_pages * 4, c->st);
+            uint16_t* dnr = dhdr[i]->as<uint16_t>();
+            launch_gather_host_pages(t.columns[i].pages, d.num_pages, d.pages->as<uint8_t>(), dnr,
+                                     dnr + d.num_pages, c->st);
+        }
+        for (uint32_t i = 0; i < t.num_columns; ++i) {
+            if (!dhdr[i]) continue;
+            const uint64_t np = dt->cols[i].num_pages;
+            hnr[i].resize(np);
+            hnn[i].resize(np);
+            HJ_CUDA(cudaMemcpyAsync(hnr[i].data(), dhdr[i]->p, np * 2, cudaMemcpyDeviceToHost, c->st));
+            HJ_CUDA(cudaMemcpyAsync(hnn[i].data(), dhdr[i]->as<uint16_t>() + np, np * 2, cudaMemcpyDeviceToHost,
+                                    c->st));
+        }
+        HJ_CUDA(cudaStreamSynchronize(c->st));
+        for (uint32_t i = 0; i < t.num_columns; ++i)
+            if (dt->cols[i].pages) page_stats(dt->cols[i], hnr[i].data(), hnn[i].data());
+        return dt;
+    }
     std::vector<uint16_t> nr, nn;
     for (uint32_t i = 0; i < t.num_columns; ++i) {
         DevColumn& d = dt->cols[i];
@@ -730,6 +765,12 @@ hj_context* hj_context_create(int device) {
         uint64_t keep = ~0ull;  // keep freed blocks for reuse
         HJ_CUDA(cudaMemPoolSetAttribute(mp, cudaMemPoolAttrReleaseThreshold, &keep));
         HJ_CUDA(cudaMallocHost(&c->pinned, 64 * sizeof(uint64_t)));
+        int pageable = 0;
+        if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device) != cudaSuccess) {
+            cudaGetLastError();
+            pageable = 0;
+        }
+        c->ats_capable = pageable != 0;
         const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
         c->pool           = std::make_unique<hj::ThreadPool>(std::min(hw, 16u) - 1);
     } catch (const hj::Error& e) {
@@ -774,6 +815,8 @@ int hj_set_option(hj_context* c, const char* name, int64_t v) {
     } else if (n == "dir_cap_bits") {
         if (v < 0 || v > 32) return HJ_ERR_INVALID;
         c->dir_cap_bits = v;
+    } else if (n == "host_access") {
+        c->host_access = v != 0;
     } else {
         c->err = "unknown option " + n;
         return HJ_ERR_INVALID;
@@ -790,6 +833,8 @@ int hj_get_option(const hj_context* c, const char* name, int64_t* v) {
     else if (n == "light_max") *v = c->light_max;
     else if (n == "timing") *v = c->timing;
     else if (n == "dir_cap_bits") *v = c->dir_cap_bits;
+    else if (n == "host_access") *v = c->host_access;
+    else if (n == "host_access_capable") *v = c->ats_capable;
     else return HJ_ERR_INVALID;
     return HJ_OK;
 }
@@ -903,7 +948,13 @@ int hj_result_copy_pages(hj_context* c, const hj_result* r, uint32_t col, void* 
     if (!c || !r || col >= r->cols.size()) return HJ_ERR_INVALID;
     return hj::guarded(c, [&] {
         const auto& oc = r->cols[col];
-        if (oc.num_pages) hj::download_pages(c, oc.pages->as<uint8_t>(), oc.num_pages, dst, nullptr);
+        if (!oc.num_pages) return;
+        if (hj::direct_host_access(c)) {
+            hj::launch_scatter_host_pages(oc.pages->as<uint8_t>(), oc.num_pages, dst, nullptr, c->st);
+            HJ_CUDA(cudaStreamSynchronize(c->st));
+        } else {
+            hj::download_pages(c, oc.pages->as<uint8_t>(), oc.num_pages, dst, nullptr);
+        }
     });
 }
 
@@ -911,8 +962,13 @@ int hj_result_copy_contiguous(hj_context* c, const hj_result* r, uint32_t col, v
     if (!c || !r || col >= r->cols.size()) return HJ_ERR_INVALID;
     return hj::guarded(c, [&] {
         const auto& oc = r->cols[col];
-        if (oc.num_pages)
+        if (!oc.num_pages) return;
+        if (hj::direct_host_access(c)) {
+            hj::launch_scatter_host_pages(oc.pages->as<uint8_t>(), oc.num_pages, nullptr, dst, c->st);
+            HJ_CUDA(cudaStreamSynchronize(c->st));
+        } else {
             hj::download_pages(c, oc.pages->as<uint8_t>(), oc.num_pages, nullptr, static_cast<uint8_t*>(dst));
+        }
     });
 }
 

@@ -20,6 +20,15 @@ T* dalloc_n(size_t n, cudaStream_t st) {
     return static_cast<T*>(dalloc(n * sizeof(T) + 16, st));
 }
 
+// ---- host <-> HBM page transfers by the GPU (hj_transfer.cu) ---------------
+// Need pageable host memory access (cudaDevAttrPageableMemoryAccess).  gather:
+// host pages -> contiguous HBM, page header fields into nr / nn (device arrays).
+void launch_gather_host_pages(const void* const* host_pages, uint64_t n, uint8_t* dst, uint16_t* nr,
+                              uint16_t* nn, cudaStream_t st);
+// scatter: contiguous HBM pages -> host_pages[i] (or host_contig when host_pages is null).
+void launch_scatter_host_pages(const uint8_t* src, uint64_t n, void* const* host_pages, void* host_contig,
+                               cudaStream_t st);
+
 // ---- scans (hj_scan.cu) ---------------------------------------------------
 // out[i] = sum(in[0..i)), out[n] = total.  out has n + 1 slots.
 void scan_exclusive_u32_to_u64(const uint32_t* in, uint64_t* out, uint64_t n, cudaStream_t st);

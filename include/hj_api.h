@@ -127,7 +127,10 @@ void* hj_context_stream(hj_context* ctx);
  * build, 0..12), "probe_group" (threads per probe key: 1, 4, 8 or 32),
  * "light_max" (largest bucket scanned by one probe group before the bucket is
  * handed to a whole block), "timing" (1: record per-phase device times of
- * each hj_execute, read with hj_result_phase_ms). */
+ * each hj_execute, read with hj_result_phase_ms), "host_access" (1, default:
+ * where the GPU can read and write pageable host memory, it moves input and
+ * result pages itself; 0: host threads stage them through pinned memory).
+ * hj_get_option("host_access_capable") reports whether the device can. */
 int hj_set_option(hj_context* ctx, const char* name, int64_t value);
 int hj_get_option(const hj_context* ctx, const char* name, int64_t* value);
 

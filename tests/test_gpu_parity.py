@@ -121,6 +121,22 @@ def test_resident_tables_give_the_same_result(engine, orc, hj):
         assert s[:3] == sh[:3] and np.array_equal(s[3], sh[3])
 
 
+def test_host_transfer_paths_agree(engine, orc):
+    """Pages moved by the GPU over host memory access and pages staged by host
+    threads through pinned memory give the same result."""
+    from hjgb300 import workloads
+    w = workloads.c2(0.01)
+    want = orc.summary(orc.run(orc.port(), w.plan))
+    saved = engine.get_option("host_access")
+    try:
+        for v in (0, 1):
+            engine.set_option("host_access", v)
+            got = orc.summary(gpu_out(orc, engine.execute(w.plan)))
+            assert got[:3] == want[:3] and np.array_equal(got[3], want[3]), v
+    finally:
+        engine.set_option("host_access", saved)
+
+
 def test_error_classes(engine, hj):
     p = hj.Plan()
     t = cases.table(hj, [["a"], ["b"]], [cases.V])
