@@ -232,7 +232,8 @@ def run_ours(args, d: Dist) -> dict:
     dir_bits = max(0, int(np.ceil(np.log2(max(1, nb)))))
     D = (1 << dir_bits) + 1
     a_probe = 4 * npr + 8 * D + 8 * nb + 8 * nout
-    t_probe = phases.get("probe", 0.0) / 1e3
+    # the probe kernels: count + write, without the host readback between them
+    t_probe = (phases.get("probe", 0.0) + phases.get("probe_write", 0.0)) / 1e3
     peak, peak_kind = peaks()
     achieved = a_probe / t_probe / 1e9 if t_probe > 0 else None
     roofline = {"bound": "hbm", "kernel": "probe (k_probe_count + k_write_*)", "achieved": achieved,

@@ -247,7 +247,7 @@ class Result:
     output_rows: int = 0
     phases: dict = field(default_factory=dict)  # device ms per phase (option "timing")
 
-PHASES = ("upload", "decode", "build", "probe", "materialize", "total", "launches")
+PHASES = ("upload", "decode", "build", "probe", "probe_sync", "probe_write", "materialize", "total", "launches")
 
 
 class Engine:

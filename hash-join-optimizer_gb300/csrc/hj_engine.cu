@@ -590,10 +590,12 @@ struct Exec {
         prm.light_max = int(c->light_max);
         prm.group     = int(c->probe_group);
         prm.pinned    = c->pinned;
+        prm.after_count = [this] { phase("probe_sync"); };
         ProbePlan* pp = nullptr;
         uint64_t total = 0;
         try {
             total = probe_count(t, pkc, prm, &pp, c->st);
+            phase("probe_write");
             if (total > 0xffffffffull) throw Error(HJ_ERR_INVALID, "join result exceeds 2^32 rows");
             out.rows = total;
             std::vector<RidOut> ro;

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <functional>
 
 #include "hj_common.cuh"
 
@@ -92,6 +93,7 @@ struct ProbeParams {
     int       light_max = 32;       // larger buckets are not scanned by one thread
     int       group     = 8;        // threads per probe key in the write pass (1, 4, 8, 32)
     uint64_t* pinned    = nullptr;  // >= 8 words of pinned host memory for count readback
+    std::function<void()> after_count;  // called once the count kernels are enqueued
 };
 
 struct ProbePlan;  // opaque match list between the count and write passes

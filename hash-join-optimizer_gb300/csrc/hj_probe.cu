@@ -394,6 +394,7 @@ uint64_t probe_count(const Table& t, const KeyCol& pk, const ProbeParams& prm, P
     HJ_LAUNCH_CHECK();
     k_mixed_count<<<kSMs * 2, 512, 0, st>>>(T, L);
     HJ_LAUNCH_CHECK();
+    if (prm.after_count) prm.after_count();
     pp->host = prm.pinned;
     HJ_CUDA(cudaMemcpyAsync(pp->host, L.ctr, 6 * sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
     HJ_CUDA(cudaStreamSynchronize(st));

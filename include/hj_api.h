@@ -160,7 +160,9 @@ int hj_result_copy_contiguous(hj_context* ctx, const hj_result* res, uint32_t co
 int  hj_result_stats(const hj_result* res, uint64_t* build_tuples, uint64_t* probe_tuples,
                      uint64_t* output_rows);
 /* Device milliseconds of one phase of the hj_execute that made `res` (option
- * "timing" = 1): "upload", "decode", "build", "probe", "materialize", "total".
+ * "timing" = 1): "upload", "decode", "build", "probe" (count kernels),
+ * "probe_sync" (match-count readback), "probe_write" (match emission),
+ * "materialize", "total".
  * Phase "launches" gives the number of kernels that hj_execute launched. */
 int  hj_result_phase_ms(const hj_result* res, const char* phase, double* ms);
 void hj_result_free(hj_result* res);
