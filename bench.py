@@ -44,7 +44,11 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["c1", "c2", "c3"], default="c2")
+    ap.add_argument("--workload", choices=["c1", "c2", "c3", "c4"], default="c2")
+    ap.add_argument("--instances", type=int, default=4096, help="c4: batch instances")
+    ap.add_argument("--wave-rows", type=int, default=1 << 32, help="c4: input rows per wave")
+    ap.add_argument("--plain-instances", type=int, default=-1,
+                    help="c4: instances timed on the plain path (-1 = all)")
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--cpu-sample", type=int, default=2_000_000,
                     help="probe rows of the bounded CPU-baseline sample")
@@ -311,6 +315,67 @@ def run_ours(args, d: Dist) -> dict:
     }
 
 
+def run_batch(args, d: Dist) -> dict:
+    """c4: the batched form against the plain one-query-at-a-time path."""
+    import numpy as np
+    import torch
+    from __graft_entry__ import load
+
+    hj = load()
+    from hjgb300 import batch, workloads
+    torch.cuda.set_device(d.local)
+    eng = hj.Engine(d.local)
+    stream = torch.cuda.ExternalStream(eng.stream)
+    w = workloads.c4(n=args.instances, scale=args.scale)
+
+    def timer(fn):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        out = fn()
+        b.record(stream)
+        b.synchronize()
+        return out, a.elapsed_time(b) / 1e3
+
+    # warm-up: whole passes (the memory pools grow to the largest wave here)
+    for _ in range(args.warmup):
+        batch.run(eng, w, hj.BATCH_PERSISTENT, args.wave_rows, torch, timer)
+    npl = len(w) if args.plain_instances < 0 else min(len(w), args.plain_instances)
+    wp = w.subset(np.arange(npl))
+    batch.run(eng, wp, hj.BATCH_PLAIN, args.wave_rows, torch, timer)
+    with Clocks(d.local) as clk:
+        d.barrier()
+        secs, redo = 0.0, 0
+        for _ in range(args.steps):
+            rows, sums, k, t = batch.run(eng, w, hj.BATCH_PERSISTENT, args.wave_rows, torch, timer)
+            secs += t
+            redo += k
+        d.barrier()
+    clocks = clk.summary()
+    t_batch = d.max(secs / args.steps)
+    # plain path: every instance (or a prefix) once, compared instance by instance
+    prow, psum, _, t_plain = batch.run(eng, wp, hj.BATCH_PLAIN, args.wave_rows, torch, timer)
+    t_plain = d.max(t_plain)
+    same = bool(np.array_equal(prow, rows[:npl]) and np.array_equal(psum, sums[:npl]))
+    eng.close()
+    q_batch = len(w) * d.world / t_batch
+    q_plain = npl * d.world / t_plain
+    probe_rows = int(w.probe_rows.sum())
+    return {
+        "metric": "batched queries/s", "value": q_batch, "unit": "queries/s", "n_gpus": d.world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_batch * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic (instances generated on the device per (seed, id), in waves; generation untimed)",
+        "config": {"workload": f"c4: {len(w)} independent 2-4-way INT32 join chains, builds log-uniform "
+                               f"{int(w.build_rows.min())}-{int(w.build_rows.max())} rows, probe 10x build",
+                   "instances": len(w), "build_rows": int(w.build_rows.sum()), "probe_rows": probe_rows,
+                   "waves": len(batch.waves(w, args.wave_rows)), "wave_rows": args.wave_rows,
+                   "l2": "inputs larger than L2"},
+        "plain": {"value": q_plain, "unit": "queries/s", "instances": npl, "seconds": t_plain},
+        "speedup_vs_plain": q_batch / q_plain, "results_equal_plain": same, "recomputed": redo,
+        "probe_tuples_per_s": probe_rows / t_batch, "clocks": clocks,
+    }
+
+
 def run_reference(args, d: Dist):
     if d.rank != 0:
         return None
@@ -339,7 +404,12 @@ def run_reference(args, d: Dist):
 def main():
     args = parse()
     d = Dist()
-    line = run_reference(args, d) if args.impl == "reference" else run_ours(args, d)
+    if args.impl == "reference":
+        line = run_reference(args, d)
+    elif args.workload == "c4":
+        line = run_batch(args, d)
+    else:
+        line = run_ours(args, d)
     if d.rank == 0 and line is not None:
         print(json.dumps(line), flush=True)
     d.close()

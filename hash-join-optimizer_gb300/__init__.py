@@ -33,7 +33,9 @@ EXPORTS = [
     "hj_result_copy_contiguous", "hj_result_stats", "hj_result_phase_ms", "hj_result_free",
     "hj_table_build", "hj_table_info", "hj_table_probe", "hj_table_free",
     "hj_pages_from_int32", "hj_pages_from_strings", "hj_table_probe_noalloc",
+    "hj_batch_execute", "hj_batch_generate",
 ]
+BATCH_PERSISTENT, BATCH_PLAIN = 0, 1
 NOALLOC_MAX_PROBE_ROWS = 65536  # HJ_NOALLOC_MAX_PROBE_ROWS
 
 
@@ -69,6 +71,14 @@ class NodeDesc(C.Structure):
 class PlanDesc(C.Structure):
     _fields_ = [("num_nodes", C.c_uint32), ("nodes", C.POINTER(NodeDesc)),
                 ("num_inputs", C.c_uint32), ("inputs", C.POINTER(TableDesc)), ("root", C.c_uint64)]
+
+
+class BatchRelation(C.Structure):
+    _fields_ = [("keys", C.c_void_p), ("payload", C.c_void_p), ("rows", C.c_uint64)]
+
+
+class BatchInstance(C.Structure):
+    _fields_ = [("num_relations", C.c_uint32), ("relations", C.POINTER(BatchRelation))]
 
 
 _lib: Optional[C.CDLL] = None
@@ -111,6 +121,8 @@ def lib() -> C.CDLL:
     L.hj_table_probe_noalloc.argtypes = [vp, vp, vp, vp, u64, vp, vp, u64, P(u64)]
     L.hj_pages_from_int32.argtypes = [vp, vp, u64, vp, u64, P(u64)]
     L.hj_pages_from_strings.argtypes = [vp, vp, vp, u64, vp, u64, P(u64)]
+    L.hj_batch_execute.argtypes = [vp, P(BatchInstance), u32, i32, P(u64), P(u64), P(u32)]
+    L.hj_batch_generate.argtypes = [vp, u64, u32, u32, u64, u32, u64, vp, vp]
     L.hj_context_destroy.restype = None
     L.hj_result_free.restype = None
     L.hj_table_free.restype = None
@@ -344,6 +356,29 @@ class Engine:
 
     def free_result(self, res: int) -> None:
         lib().hj_result_free(res)
+
+    def batch_generate(self, seed: int, instance: int, relation: int, build_rows: int, match_q24: int,
+                       rows: int, keys: int, payload: int) -> None:
+        """hj_batch_generate: one synthetic relation into device buffers (enqueued on `stream`)."""
+        _check(self._ctx, lib().hj_batch_generate(self._ctx, seed, instance, relation, build_rows, match_q24,
+                                                  rows, keys, payload))
+
+    def batch_execute(self, instances: Sequence[Sequence[tuple]], mode: int = BATCH_PERSISTENT):
+        """hj_batch_execute over instances given as [(keys ptr, payload ptr, rows), ...]
+        per relation (device pointers).  Returns (rows uint64[n], checksums uint64[n],
+        instances recomputed on the plain path)."""
+        n = len(instances)
+        rels = [(BatchRelation * len(inst))(*[BatchRelation(k, p, r) for k, p, r in inst]) for inst in instances]
+        arr = (BatchInstance * max(1, n))()
+        for i, r in enumerate(rels):
+            arr[i].num_relations, arr[i].relations = len(r), r
+        rows = np.zeros(max(1, n), dtype=np.uint64)
+        sums = np.zeros(max(1, n), dtype=np.uint64)
+        redo = C.c_uint32()
+        _check(self._ctx, lib().hj_batch_execute(self._ctx, arr, n, mode,
+                                                 rows.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                                 sums.ctypes.data_as(C.POINTER(C.c_uint64)), C.byref(redo)))
+        return rows[:n], sums[:n], redo.value
 
     def execute(self, plan: Plan) -> Result:
         """Contest::execute: runs the plan and returns the root's pages on the host."""

@@ -206,6 +206,9 @@ struct hj_context {
     int64_t             dir_cap_bits = 22;  // automatic directories stay <= 32 MB (L2 resident)
     bool                ats_capable  = false;  // GPU reads/writes pageable host memory
     int64_t             host_access  = 1;      // use it for page transfers when capable
+    int64_t             batch_load_pct = 50;   // batched joins: build rows per 100 buckets of a partition table
+    int64_t             batch_graph    = 1;    // batched joins: launch as one CUDA graph
+    int64_t             batch_part_log2 = 12;  // batched joins: ~2^x build rows per partition
     uint64_t*           pinned      = nullptr;  // small readbacks
     uint8_t*            staging     = nullptr;  // pinned transfer ring
     size_t              staging_bytes = 0;
@@ -819,6 +822,14 @@ int hj_set_option(hj_context* c, const char* name, int64_t v) {
         c->dir_cap_bits = v;
     } else if (n == "host_access") {
         c->host_access = v != 0;
+    } else if (n == "batch_load_pct") {
+        if (v < 10 || v > 800) return HJ_ERR_INVALID;
+        c->batch_load_pct = v;
+    } else if (n == "batch_graph") {
+        c->batch_graph = v != 0;
+    } else if (n == "batch_part_log2") {
+        if (v < 8 || v > 13) return HJ_ERR_INVALID;
+        c->batch_part_log2 = v;
     } else {
         c->err = "unknown option " + n;
         return HJ_ERR_INVALID;
@@ -837,6 +848,9 @@ int hj_get_option(const hj_context* c, const char* name, int64_t* v) {
     else if (n == "dir_cap_bits") *v = c->dir_cap_bits;
     else if (n == "host_access") *v = c->host_access;
     else if (n == "host_access_capable") *v = c->ats_capable;
+    else if (n == "batch_load_pct") *v = c->batch_load_pct;
+    else if (n == "batch_graph") *v = c->batch_graph;
+    else if (n == "batch_part_log2") *v = c->batch_part_log2;
     else return HJ_ERR_INVALID;
     return HJ_OK;
 }
@@ -1067,6 +1081,51 @@ int hj_table_probe(hj_context* c, const hj_hash_table* t, const int32_t* keys, c
     if (rc != HJ_OK) return rc;
     if (status != HJ_OK) c->err = "output capacity too small";
     return status;
+}
+
+int hj_batch_execute(hj_context* c, const hj_batch_instance* inst, uint32_t n, int32_t mode, uint64_t* rows,
+                     uint64_t* checksums, uint32_t* recomputed) {
+    if (!c || (n > 0 && (!inst || !rows || !checksums))) return HJ_ERR_INVALID;
+    if (mode != HJ_BATCH_PERSISTENT && mode != HJ_BATCH_PLAIN) return HJ_ERR_INVALID;
+    if (recomputed) *recomputed = 0;
+    return hj::guarded(c, [&] {
+        std::vector<hj::BatchInstance> B(n);
+        for (uint32_t i = 0; i < n; ++i) {
+            if (inst[i].num_relations < 2 || !inst[i].relations)
+                throw hj::Error(HJ_ERR_INVALID, "batch instance " + std::to_string(i) + " needs >= 2 relations");
+            for (uint32_t r = 0; r < inst[i].num_relations; ++r) {
+                const hj_batch_relation& x = inst[i].relations[r];
+                B[i].rels.push_back({x.keys, x.payload, x.rows});
+            }
+        }
+        const hj::ProbeParams prm = hj::context_probe_params(c);
+        auto plain = [&](uint32_t i) {
+            hj::plain_instance(B[i], prm, int(c->dir_bits), int(c->radix_bits), int(c->dir_cap_bits), rows[i],
+                               checksums[i], c->st);
+        };
+        if (mode == HJ_BATCH_PLAIN) {
+            for (uint32_t i = 0; i < n; ++i) plain(i);
+            return;
+        }
+        hj::BatchOptions o;
+        o.load       = double(c->batch_load_pct) / 100.0;
+        o.graph      = c->batch_graph != 0;
+        o.part_rows_log2 = int(c->batch_part_log2);
+        std::vector<uint64_t> r, s;
+        const std::vector<uint32_t> redo = hj::batch_execute(B, o, r, s, c->st);
+        std::copy(r.begin(), r.end(), rows);
+        std::copy(s.begin(), s.end(), checksums);
+        for (uint32_t i : redo) plain(i);
+        if (recomputed) *recomputed = uint32_t(redo.size());
+    });
+}
+
+int hj_batch_generate(hj_context* c, uint64_t seed, uint32_t instance, uint32_t relation, uint64_t build_rows,
+                      uint32_t match_q24, uint64_t rows, int32_t* keys, int32_t* payload) {
+    if (!c) return HJ_ERR_INVALID;
+    return hj::guarded(c, [&] {
+        hj::launch_batch_generate(seed, instance, relation, build_rows, match_q24, rows, keys, payload, c->st);
+    });
 }
 
 void hj_table_free(hj_hash_table* t) {

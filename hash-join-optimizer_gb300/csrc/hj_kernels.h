@@ -6,6 +6,7 @@
 
 #include <cstdint>
 #include <functional>
+#include <vector>
 
 #include "hj_common.cuh"
 
@@ -35,7 +36,7 @@ void launch_scatter_host_pages(const uint8_t* src, uint64_t n, void* const* host
 void scan_exclusive_u32_to_u64(const uint32_t* in, uint64_t* out, uint64_t n, cudaStream_t st);
 void scan_exclusive_u64(const uint64_t* in, uint64_t* out, uint64_t n, cudaStream_t st);
 // Same as scan_exclusive_u32_to_u64 with caller-provided temporaries of
-// scan_tmp_words(n) words (n <= 4096^2); allocates nothing.
+// scan_tmp_words(n) words; allocates nothing (so it can be graph-captured).
 size_t scan_tmp_words(uint64_t n);
 void   scan_exclusive_u32_to_u64_into(const uint32_t* in, uint64_t* out, uint64_t n, uint64_t* tmp,
                                       cudaStream_t st);
@@ -102,7 +103,8 @@ struct ProbePlan;  // opaque match list between the count and write passes
 uint64_t probe_count(const Table& t, const KeyCol& pk, const ProbeParams& prm, ProbePlan** pp,
                      cudaStream_t st);
 // Write pass: emits the row-id streams for the matches found by probe_count
-// (all `nout` streams have probe_count() slots) and frees *pp.
+// (all `nout` streams have probe_count() slots); the caller frees *pp with
+// probe_free afterwards.
 void probe_write(const Table& t, const KeyCol& pk, ProbePlan* pp, const RidOut* outs, int nout,
                  cudaStream_t st);
 void probe_free(ProbePlan* pp, cudaStream_t st);
@@ -140,6 +142,35 @@ struct VarcharOut {
 void     varchar_plan(VarcharOut& v, cudaStream_t st);
 // pages = tile_off[ntiles] as read by the caller; returns the page buffer.
 uint8_t* varchar_write(VarcharOut& v, uint64_t pages, cudaStream_t st);
+
+// ---- batched independent joins (hj_batch.cu) ------------------------------
+// One relation of a batch instance: INT32 keys (no NULLs) and one INT32 payload.
+struct BatchRelation {
+    const int32_t* keys;
+    const int32_t* payload;
+    uint64_t       rows;
+};
+// A chain R0 x R1 x ... on one key: R0 probes R1, the result probes R2, ...
+// (2 to 8 relations)
+struct BatchInstance {
+    std::vector<BatchRelation> rels;
+};
+struct BatchOptions {
+    double load       = 0.5;   // build rows per bucket of a partition table (2^ceil(log2(rows / load)) buckets)
+    int    part_rows_log2 = 12;  // partitions of ~2^x build rows (x in 8..13); radix bits follow per instance
+    bool   graph      = true;  // capture the whole batch in one CUDA graph
+};
+// Row count and checksum (sum of row fingerprints) per instance.  Returns the
+// instances with a partition too large for a shared-memory table (their rows /
+// sums are not valid; the caller recomputes them with plain_instance).
+std::vector<uint32_t> batch_execute(const std::vector<BatchInstance>& b, const BatchOptions& o,
+                                    std::vector<uint64_t>& rows, std::vector<uint64_t>& sums, cudaStream_t st);
+// One instance through the regular table build and two-pass probe.
+void plain_instance(const BatchInstance& b, const ProbeParams& prm, int dir_bits, int radix_bits, int dir_cap_bits,
+                    uint64_t& rows, uint64_t& sum, cudaStream_t st);
+// Synthetic instance relations generated on the device from (seed, instance, relation).
+void launch_batch_generate(uint64_t seed, uint32_t instance, uint32_t relation, uint64_t build_rows,
+                           uint32_t match_q24, uint64_t rows, int32_t* keys, int32_t* payload, cudaStream_t st);
 
 }  // namespace hj
 

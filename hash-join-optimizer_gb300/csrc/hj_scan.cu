@@ -84,30 +84,38 @@ void scan_exclusive_u64(const uint64_t* in, uint64_t* out, uint64_t n, cudaStrea
 
 size_t scan_tmp_words(uint64_t n) {
     const uint64_t blocks = (n + kScanTile - 1) / kScanTile;
-    return blocks <= 1 ? 0 : size_t(2 * blocks + 1);
+    return blocks <= 1 ? 0 : size_t(2 * blocks + 1) + scan_tmp_words(blocks);
 }
 
-void scan_exclusive_u32_to_u64_into(const uint32_t* in, uint64_t* out, uint64_t n, uint64_t* tmp,
-                                    cudaStream_t st) {
+namespace {
+
+template <class Tin>
+void scan_into_impl(const Tin* in, uint64_t* out, uint64_t n, uint64_t* tmp, cudaStream_t st) {
     if (n == 0) {
         HJ_CUDA(cudaMemsetAsync(out, 0, sizeof(uint64_t), st));
         return;
     }
     const uint64_t blocks = (n + kScanTile - 1) / kScanTile;
     if (blocks == 1) {
-        k_scan_apply<uint32_t><<<1, kScanThreads, 0, st>>>(in, out, n, nullptr);
+        k_scan_apply<Tin><<<1, kScanThreads, 0, st>>>(in, out, n, nullptr);
         HJ_LAUNCH_CHECK();
         return;
     }
-    if (blocks > uint64_t(kScanTile)) throw Error(HJ_ERR_INVALID, "scan too large for a two-level scan");
+    if (blocks > 0x7fffffffull) throw Error(HJ_ERR_INVALID, "scan too large");
     uint64_t* sums = tmp;
     uint64_t* offs = tmp + blocks;
-    k_block_sums<uint32_t><<<unsigned(blocks), kScanThreads, 0, st>>>(in, n, sums);
+    k_block_sums<Tin><<<unsigned(blocks), kScanThreads, 0, st>>>(in, n, sums);
     HJ_LAUNCH_CHECK();
-    k_scan_apply<uint64_t><<<1, kScanThreads, 0, st>>>(sums, offs, blocks, nullptr);
+    scan_into_impl<uint64_t>(sums, offs, blocks, tmp + 2 * blocks + 1, st);
+    k_scan_apply<Tin><<<unsigned(blocks), kScanThreads, 0, st>>>(in, out, n, offs);
     HJ_LAUNCH_CHECK();
-    k_scan_apply<uint32_t><<<unsigned(blocks), kScanThreads, 0, st>>>(in, out, n, offs);
-    HJ_LAUNCH_CHECK();
+}
+
+}  // namespace
+
+void scan_exclusive_u32_to_u64_into(const uint32_t* in, uint64_t* out, uint64_t n, uint64_t* tmp,
+                                    cudaStream_t st) {
+    scan_into_impl<uint32_t>(in, out, n, tmp, st);
 }
 
 }  // namespace hj

@@ -199,3 +199,54 @@ def c3(scale: float = 1.0, seed: int = 42) -> Workload:
     # every R1 row reaches exactly one row of each later relation
     return Workload("c3", plan, int(kept_rows[0].size), int(sum(x.size for x in kept_rows[1:])),
                     expected_rows=int(kept_rows[0].size), meta=meta)
+
+
+# ----------------------------------------------------------- batched (c4) --
+
+@dataclass
+class BatchWorkload:
+    """Independent join chains R0 x R1 x ... on one INT32 key (hj_batch_execute).
+    Instance i has relations[i] relations; R1.. hold build_rows[i] distinct keys,
+    R0 probe_rows[i] keys of which a fraction match_q24[i] / 2^24 hit R1.  The
+    relations themselves are generated on the device (hj_batch_generate),
+    keyed by (seed, instance id)."""
+    name: str
+    seed: int
+    relations: np.ndarray
+    build_rows: np.ndarray
+    probe_rows: np.ndarray
+    match_q24: np.ndarray
+    ids: Optional[np.ndarray] = None  # instance ids (default 0..n-1)
+
+    def __len__(self) -> int:
+        return int(self.relations.size)
+
+    def instance_id(self, i: int) -> int:
+        return int(self.ids[i]) if self.ids is not None else int(i)
+
+    def instance(self, i: int):
+        """(instance id, relations, build rows, match_q24, probe rows)."""
+        return (self.instance_id(i), int(self.relations[i]), int(self.build_rows[i]), int(self.match_q24[i]),
+                int(self.probe_rows[i]))
+
+    def rows(self, i: int) -> int:
+        """input rows of instance i (all relations)."""
+        return int(self.probe_rows[i] + (self.relations[i] - 1) * self.build_rows[i])
+
+    def subset(self, idx) -> "BatchWorkload":
+        idx = np.asarray(idx, dtype=np.int64)
+        ids = self.ids[idx] if self.ids is not None else idx
+        return BatchWorkload(self.name, self.seed, self.relations[idx], self.build_rows[idx], self.probe_rows[idx],
+                             self.match_q24[idx], ids)
+
+
+def c4(n: int = 4096, seed: int = 42, scale: float = 1.0, lo: int = 1_000, hi: int = 4_000_000) -> BatchWorkload:
+    """4,096 independent 2- to 4-way INT32 equi-joins: build sizes log-uniform in
+    [1k, 4M] rows (times `scale`), every probe side 10x its build size, match
+    rate uniform in [10%, 100%], one INT32 payload per relation."""
+    r = _rng(seed, 4)
+    b = np.exp(r.uniform(np.log(lo), np.log(hi), size=n))
+    b = np.maximum(1, np.round(b * scale)).astype(np.int64)
+    m = r.integers(2, 5, size=n).astype(np.int64)
+    q = np.round(r.uniform(0.10, 1.00, size=n) * (1 << 24)).astype(np.int64)
+    return BatchWorkload("c4", seed, m, b, 10 * b, q)

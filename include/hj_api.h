@@ -209,6 +209,47 @@ int hj_table_probe_noalloc(hj_context* ctx, const hj_hash_table* t, const int32_
                            const uint32_t* valid, uint64_t n, uint32_t* out_probe_rows,
                            uint32_t* out_build_rows, uint64_t capacity, uint64_t* num_matches);
 
+/* ---- batched independent joins ----------------------------------------------
+ * Many independent INT32 join chains in one call: instance i joins its
+ * relations R0 x R1 x ... x Rm-1 (2 <= m <= 8) on one key (R0 probes R1, the
+ * result probes R2, ...).  Every relation is (key, payload) INT32 columns in
+ * HBM without NULLs.  Per instance the call returns the result row count and a
+ * checksum: the sum mod 2^64 over the result rows of a 64-bit fingerprint
+ * folded over (key, payload of R0, ..., payload of Rm-1).
+ *   mode HJ_BATCH_PERSISTENT: all relations of all instances radix-partitioned
+ *     together on the key (partitions of ~2^batch_part_log2 build rows), then
+ *     per (instance, partition) the build relations become shared-memory
+ *     tables and R0's rows run through the whole chain -- persistent kernels
+ *     over device-side work queues, the whole batch launched as one CUDA graph
+ *     (options batch_part_log2, batch_load_pct, batch_graph).  Instances with
+ *     a partition too large for shared memory (heavy duplicate keys) are
+ *     recomputed with the plain path; *recomputed (may be NULL) counts them.
+ *   mode HJ_BATCH_PLAIN: the instances one after another through the regular
+ *     build / probe (options dir_bits, radix_bits, dir_cap_bits, probe_group,
+ *     light_max) -- the one-query-at-a-time comparison.
+ * Synchronous.  No counterpart in the reference (its execute() runs one plan). */
+typedef struct hj_batch_relation {
+    const int32_t* keys;
+    const int32_t* payload;
+    uint64_t       rows;
+} hj_batch_relation;
+typedef struct hj_batch_instance {
+    uint32_t                 num_relations;
+    const hj_batch_relation* relations;
+} hj_batch_instance;
+enum { HJ_BATCH_PERSISTENT = 0, HJ_BATCH_PLAIN = 1 };
+int hj_batch_execute(hj_context* ctx, const hj_batch_instance* instances, uint32_t n, int32_t mode,
+                     uint64_t* rows, uint64_t* checksums, uint32_t* recomputed);
+/* Synthetic relation of a batch instance, generated in HBM from (seed,
+ * instance, relation), enqueued on the context stream (hj_context_stream).
+ * Build relations (relation >= 1): `rows` <= build_rows distinct keys in
+ * [0, 2 build_rows).  Relation 0 (probe): `rows` keys, each one of R1's keys
+ * with probability match_q24 / 2^24, else a key R1 does not hold.  Payloads
+ * are uniform 32-bit values. */
+int hj_batch_generate(hj_context* ctx, uint64_t seed, uint32_t instance, uint32_t relation,
+                      uint64_t build_rows, uint32_t match_q24, uint64_t rows, int32_t* keys,
+                      int32_t* payload);
+
 /* ---- host page writers (Table::to_columnar / ColumnInserter packing) ----- */
 
 /* INT32 column of n rows into pages: valid (one byte per row, 0 = NULL) may be

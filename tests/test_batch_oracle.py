@@ -1,0 +1,113 @@
+"""The batched-join oracle (oracle/batch_oracle.py) on the CPU: generator
+properties, and chain results against the compiled reference's execute() and
+the CPU restatement of it, run on the same relations as a left-deep plan."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import batch_oracle as bo
+
+
+def chain_plan(hj, rels):
+    """Left-deep plan over [(keys, payload), ...]: output key, p0, ..., pm-1."""
+    p = hj.Plan()
+    for k, v in rels:
+        p.new_input(hj.Table(k.size, [hj.Column.int32(k), hj.Column.int32(v)]))
+    scans = [p.new_scan_node(j, [(0, hj.INT32), (1, hj.INT32)]) for j in range(len(rels))]
+    cur, width = scans[0], 2
+    for j in range(1, len(rels)):
+        attrs = [(c, hj.INT32) for c in range(width)] + [(width + 1, hj.INT32)]
+        cur = p.new_join_node(False, cur, scans[j], 0, 0, attrs)
+        width += 1
+    p.root = cur
+    return p
+
+
+def plan_result(orc, lib, plan, m):
+    out = orc.run(lib, plan)
+    assert out.status == 0, out.error
+    dec = orc.decode(out.columns)
+    if out.num_rows == 0:
+        return 0, 0
+    cols = [d[0] for _, d in dec]
+    assert all(np.all(d[1]) for _, d in dec)  # no NULLs
+    fp = bo.row_fingerprints(cols[0], np.array(cols[1:], dtype=np.int32).reshape(m, -1))
+    return out.num_rows, int(fp.sum(dtype=np.uint64))
+
+
+def test_generator_properties():
+    seed, b, q = 42, 5000, int(0.3 * (1 << 24))
+    keys1, _ = bo.relation(seed, 7, 1, b, q, b)
+    assert np.unique(keys1).size == b and keys1.min() >= 0 and keys1.max() < 2 * b
+    keys0, pay0 = bo.relation(seed, 7, 0, b, q, 10 * b)
+    hit = np.isin(keys0, keys1)
+    assert abs(hit.mean() - 0.3) < 0.02
+    assert keys0.min() >= 0 and keys0.max() < 2 * b
+    # payloads differ across relations and instances
+    _, pay0b = bo.relation(seed, 8, 0, b, q, 10 * b)
+    assert not np.array_equal(pay0, pay0b)
+    # fewer build rows than build_rows: a prefix of the same keys
+    k_short, _ = bo.relation(seed, 7, 1, b, q, 100)
+    assert np.array_equal(k_short, keys1[:100])
+
+
+def test_fold_known_values():
+    """The fingerprint on fixed inputs (Python ints, independent of numpy)."""
+    def fin(x):
+        x &= bo.M64
+        x = ((x ^ (x >> 30)) * 0xBF58476D1CE4E5B9) & bo.M64
+        x = ((x ^ (x >> 27)) * 0x94D049BB133111EB) & bo.M64
+        return x ^ (x >> 31)
+
+    def add(st, v):
+        return ((st ^ (v & 0xFFFFFFFF)) * bo.GOLD) & bo.M64
+
+    key, p0, p1 = -5, 7, -(2**31)
+    st = (((key & 0xFFFFFFFF) ^ 0x243F6A8885A308D3) * bo.GOLD) & bo.M64
+    want = fin(add(add(st, p0), p1))
+    got = bo.row_fingerprints(np.array([key], np.int32), np.array([[p0], [p1]], np.int32))
+    assert int(got[0]) == want
+    # a different pairing of the same values gives a different fingerprint
+    other = bo.row_fingerprints(np.array([key], np.int32), np.array([[p1], [p0]], np.int32))
+    assert int(other[0]) != want
+
+
+@pytest.mark.parametrize("m,b,rate", [(2, 300, 0.5), (3, 800, 1.0), (4, 1500, 0.1), (2, 1, 1.0)])
+def test_chain_result_matches_reference_execute(hj, orc, m, b, rate):
+    q = int(round(rate * (1 << 24)))
+    rels = bo.instance_relations(42, 11 + m, m, b, q, 10 * b)
+    want = bo.chain_result(rels)
+    plan = chain_plan(hj, rels)
+    assert plan_result(orc, orc.port(), plan, m) == want
+    ref = orc.ref()
+    if ref is None:
+        pytest.skip("reference build not available")
+    assert plan_result(orc, ref, plan, m) == want
+
+
+def test_chain_with_duplicate_keys(hj, orc):
+    """Duplicate build keys give the cross product in the oracle as in the reference."""
+    r = np.random.default_rng(3)
+    rels = [(r.integers(0, 40, 500).astype(np.int32), r.integers(-9, 9, 500).astype(np.int32)),
+            (r.integers(0, 60, 200).astype(np.int32), r.integers(-9, 9, 200).astype(np.int32)),
+            (r.integers(20, 50, 100).astype(np.int32), r.integers(-9, 9, 100).astype(np.int32))]
+    want = bo.chain_result(rels)
+    assert want[0] > 500
+    plan = chain_plan(hj, rels)
+    assert plan_result(orc, orc.port(), plan, 3) == want
+    ref = orc.ref()
+    if ref is not None:
+        assert plan_result(orc, ref, plan, 3) == want
+
+
+def test_batch_waves_cover_every_instance(hj):
+    from hjgb300 import batch, workloads
+    w = workloads.c4(n=300, scale=0.01)
+    ws = batch.waves(w, 200_000)
+    flat = [i for g in ws for i in g]
+    assert flat == list(range(len(w)))
+    for g in ws:
+        assert len(g) == 1 or sum(w.rows(i) for i in g) <= 200_000
+    s = w.subset([3, 9])
+    assert s.instance(1)[0] == 9 and s.instance(1)[1:] == w.instance(9)[1:]
