@@ -44,9 +44,14 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["c1", "c2", "c3", "c4"], default="c2")
+    ap.add_argument("--workload", choices=["c1", "c2", "c3", "c4", "c5"], default="c2")
+    ap.add_argument("--rates", default="50,100,200,500,1000,2000,5000", help="c5: offered queries/s")
+    ap.add_argument("--requests", type=int, default=200, help="c5: requests per rate")
+    ap.add_argument("--slots", type=int, default=8, help="c5: plans running at once")
+    ap.add_argument("--budget-gb", type=float, default=150.0, help="c5: HBM admission budget")
     ap.add_argument("--instances", type=int, default=4096, help="c4: batch instances")
     ap.add_argument("--wave-rows", type=int, default=1 << 32, help="c4: input rows per wave")
+    ap.add_argument("--retune", action="store_true", help="c4: ignore the autotuner cache")
     ap.add_argument("--plain-instances", type=int, default=-1,
                     help="c4: instances timed on the plain path (-1 = all)")
     ap.add_argument("--scale", type=float, default=1.0)
@@ -336,6 +341,11 @@ def run_batch(args, d: Dist) -> dict:
         b.synchronize()
         return out, a.elapsed_time(b) / 1e3
 
+    # options of both paths from the autotuner (sweeps a stratified sample)
+    from hjgb300 import autotune
+    tuned = autotune.tune(eng, w, torch=torch, cache=None if args.retune else autotune.DEFAULT_CACHE,
+                          force=args.retune)
+    autotune.apply(eng, tuned)
     # warm-up: whole passes (the memory pools grow to the largest wave here)
     for _ in range(args.warmup):
         batch.run(eng, w, hj.BATCH_PERSISTENT, args.wave_rows, torch, timer)
@@ -369,10 +379,61 @@ def run_batch(args, d: Dist) -> dict:
                                f"{int(w.build_rows.min())}-{int(w.build_rows.max())} rows, probe 10x build",
                    "instances": len(w), "build_rows": int(w.build_rows.sum()), "probe_rows": probe_rows,
                    "waves": len(batch.waves(w, args.wave_rows)), "wave_rows": args.wave_rows,
-                   "l2": "inputs larger than L2"},
+                   "l2": "inputs larger than L2",
+                   "tuned": {"batched": {k: v for k, v in tuned["batched"].items() if k != "seconds"},
+                             "plain": {k: v for k, v in tuned["plain"].items() if k != "seconds"}}},
         "plain": {"value": q_plain, "unit": "queries/s", "instances": npl, "seconds": t_plain},
         "speedup_vs_plain": q_batch / q_plain, "results_equal_plain": same, "recomputed": redo,
         "probe_tuples_per_s": probe_rows / t_batch, "clocks": clocks,
+    }
+
+
+def run_serve(args, d: Dist) -> dict:
+    """c5: the request loop against the plain one-plan-at-a-time path."""
+    import torch
+    from __graft_entry__ import load
+
+    hj = load()
+    from hjgb300 import serve
+    torch.cuda.set_device(d.local)
+    eng = hj.Engine(d.local)
+    mix = serve.c5_mix(eng, large_scale=args.scale)
+    rates = [float(x) for x in args.rates.split(",")]
+    budget = int(args.budget_gb * (1 << 30))
+    # warm-up: every plan once on each path (pools grow, cached tables get built)
+    for kind in serve.KINDS:
+        for p in mix.plans[kind]:
+            eng.free_result(eng.execute_raw(p))
+    eng.set_option("table_cache", 1)
+    for _ in range(max(1, args.warmup)):
+        serve.run_served(eng, mix, serve.schedule(mix, rates[-1], 64, seed=99), budget, args.slots)
+    lines, equal = [], True
+    with Clocks(d.local) as clk:
+        for r in rates:
+            sched = serve.schedule(mix, r, args.requests, seed=int(r))
+            eng.set_option("table_cache", 1)
+            sv = serve.run_served(eng, mix, sched, budget, args.slots)
+            eng.set_option("table_cache", 0)
+            pl = serve.run_plain(eng, mix, sched)
+            same = sv.pop("results") == pl.pop("results")
+            equal &= same
+            lines.append({"offered_qps": r, "served": sv, "plain": pl, "results_equal": same})
+    clocks = clk.summary()
+    mix.release(eng)
+    eng.close()
+    top = lines[-1]
+    return {
+        "metric": "served queries/s", "value": top["served"]["qps"], "unit": "queries/s", "n_gpus": d.world,
+        "steps": len(rates), "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic (seeded generators; base tables resident and decoded in HBM)",
+        "config": {"workload": "c5: open-loop Poisson stream, 70% small 2-way (build 10k-1M, probe 10x), "
+                               "25% c3 at 1/10, 5% c2 (16M x 256M)",
+                   "requests_per_rate": args.requests, "slots": args.slots, "hbm_budget_gb": args.budget_gb,
+                   "large_scale": args.scale},
+        "plain_qps_at_top_rate": top["plain"]["qps"], "speedup_vs_plain": top["served"]["qps"] / top["plain"]["qps"],
+        "p99_ms_at_top_rate": top["served"]["p99_ms"], "results_equal_plain": equal, "rates": lines,
+        "clocks": clocks,
     }
 
 
@@ -408,6 +469,8 @@ def main():
         line = run_reference(args, d)
     elif args.workload == "c4":
         line = run_batch(args, d)
+    elif args.workload == "c5":
+        line = run_serve(args, d)
     else:
         line = run_ours(args, d)
     if d.rank == 0 and line is not None:

@@ -33,7 +33,8 @@ EXPORTS = [
     "hj_result_copy_contiguous", "hj_result_stats", "hj_result_phase_ms", "hj_result_free",
     "hj_table_build", "hj_table_info", "hj_table_probe", "hj_table_free",
     "hj_pages_from_int32", "hj_pages_from_strings", "hj_table_probe_noalloc",
-    "hj_batch_execute", "hj_batch_generate",
+    "hj_batch_execute", "hj_batch_generate", "hj_table_prepare",
+    "hj_server_create", "hj_server_submit", "hj_server_wait", "hj_server_info", "hj_server_destroy",
 ]
 BATCH_PERSISTENT, BATCH_PLAIN = 0, 1
 NOALLOC_MAX_PROBE_ROWS = 65536  # HJ_NOALLOC_MAX_PROBE_ROWS
@@ -81,6 +82,15 @@ class BatchInstance(C.Structure):
     _fields_ = [("num_relations", C.c_uint32), ("relations", C.POINTER(BatchRelation))]
 
 
+class ServerOptions(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_uint64), ("slots", C.c_uint32)]
+
+
+class RequestStats(C.Structure):
+    _fields_ = [("queue_ms", C.c_double), ("service_ms", C.c_double), ("latency_ms", C.c_double),
+                ("est_bytes", C.c_uint64)]
+
+
 _lib: Optional[C.CDLL] = None
 
 
@@ -123,6 +133,14 @@ def lib() -> C.CDLL:
     L.hj_pages_from_strings.argtypes = [vp, vp, vp, u64, vp, u64, P(u64)]
     L.hj_batch_execute.argtypes = [vp, P(BatchInstance), u32, i32, P(u64), P(u64), P(u32)]
     L.hj_batch_generate.argtypes = [vp, u64, u32, u32, u64, u32, u64, vp, vp]
+    L.hj_table_prepare.argtypes = [vp, u64]
+    L.hj_server_create.restype = vp
+    L.hj_server_create.argtypes = [vp, P(ServerOptions)]
+    L.hj_server_submit.argtypes = [vp, P(PlanDesc), P(u64)]
+    L.hj_server_wait.argtypes = [vp, u64, P(vp), P(RequestStats), C.c_char_p, u32]
+    L.hj_server_info.argtypes = [vp, P(u64), P(u64), P(u64), P(u64)]
+    L.hj_server_destroy.argtypes = [vp]
+    L.hj_server_destroy.restype = None
     L.hj_context_destroy.restype = None
     L.hj_result_free.restype = None
     L.hj_table_free.restype = None
@@ -236,6 +254,20 @@ class Plan:
         d = PlanDesc(len(self.nodes), nodes, len(self.inputs), tables, self.root)
         return d, keep
 
+    def frozen(self) -> "FrozenPlan":
+        """The descriptor built once, for plans submitted many times unchanged."""
+        return FrozenPlan(*self.desc())
+
+
+@dataclass
+class FrozenPlan:
+    """A Plan's C-ABI descriptor, built once (Plan.frozen)."""
+    d: object
+    keep: list
+
+    def desc(self):
+        return self.d, self.keep
+
 
 def _page_ptrs(col: "Column", keep: list):
     """Array of the column's page addresses (kept alive through `keep`)."""
@@ -321,6 +353,13 @@ class Engine:
     def release(self, table: Table) -> None:
         _check(self._ctx, lib().hj_table_release(self._ctx, table.resident))
 
+    def prepare(self, table: Table) -> None:
+        """Decodes a resident table's columns once and keeps them decoded in HBM."""
+        _check(self._ctx, lib().hj_table_prepare(self._ctx, table.resident))
+
+    def server(self, hbm_budget_bytes: int, slots: int) -> "Server":
+        return Server(self, hbm_budget_bytes, slots)
+
     def execute_raw(self, plan: Plan) -> int:
         """Runs the plan and returns the opaque hj_result pointer (pages stay in HBM)."""
         d, keep = plan.desc()
@@ -387,6 +426,56 @@ class Engine:
             return self.fetch(res)
         finally:
             self.free_result(res)
+
+
+class Server:
+    """hj_server: a request loop running plans concurrently on the engine's GPU
+    against an HBM budget.  submit() returns a ticket; wait() blocks until that
+    plan ran and returns (result handle, stats dict); free results with
+    Engine.free_result, fetch them with Engine.fetch."""
+
+    def __init__(self, engine: Engine, hbm_budget_bytes: int, slots: int):
+        self.engine = engine
+        opt = ServerOptions(int(hbm_budget_bytes), int(slots))
+        self._s = lib().hj_server_create(engine.handle, C.byref(opt))
+        if not self._s:
+            msg = lib().hj_last_error(engine.handle)
+            raise HjError(HJ_ERR_INVALID, msg.decode() if msg else "hj_server_create failed")
+        self._keep = {}
+
+    def submit(self, plan: Plan) -> int:
+        d, keep = plan.desc()
+        t = C.c_uint64()
+        _check(self.engine.handle, lib().hj_server_submit(self._s, C.byref(d), C.byref(t)))
+        self._keep[t.value] = (d, keep)  # host pages of non-resident inputs stay alive until wait
+        return t.value
+
+    def wait(self, ticket: int):
+        res = C.c_void_p()
+        st = RequestStats()
+        err = C.create_string_buffer(512)
+        rc = lib().hj_server_wait(self._s, ticket, C.byref(res), C.byref(st), err, 512)
+        self._keep.pop(ticket, None)
+        if rc != HJ_OK:
+            raise HjError(rc, err.value.decode(errors="replace"))
+        return res.value, {"queue_ms": st.queue_ms, "service_ms": st.service_ms, "latency_ms": st.latency_ms,
+                           "est_bytes": st.est_bytes}
+
+    def info(self) -> dict:
+        q, r, rb, pb = C.c_uint64(), C.c_uint64(), C.c_uint64(), C.c_uint64()
+        lib().hj_server_info(self._s, C.byref(q), C.byref(r), C.byref(rb), C.byref(pb))
+        return {"queued": q.value, "running": r.value, "running_bytes": rb.value, "peak_bytes": pb.value}
+
+    def close(self) -> None:
+        if self._s:
+            lib().hj_server_destroy(self._s)
+            self._s = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
 
 # ------------------------------------------------------------ page decoding --

@@ -27,6 +27,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <tuple>
 #include <thread>
 #include <vector>
 
@@ -148,8 +149,9 @@ struct DevColumn {
     uint64_t non_null  = 0;
     bool     dense1984 = false;  // INT32, no NULLs, every page but the last 1984 rows
     int64_t  strref_bad_page = -1;  // first page index > 2^18-1 that carries strings
-    // decoded form (per execute call)
-    bool decoded = false;
+    // decoded form (per execute call, or once per resident table: predecoded)
+    bool decoded    = false;
+    bool predecoded = false;
     Buf  plain;   // INT32 without NULLs on irregular pages
     Buf  tagged;  // INT32 with NULLs: value_t per row
     Buf  locs;    // VARCHAR: locator per row
@@ -189,6 +191,48 @@ struct DevTable {
     std::vector<DevColumn> cols;
 };
 
+// Unchained tables built over a resident base column, kept for reuse by later
+// plans (option "table_cache"): keyed by the table handle, the column and the
+// options that shape the table.
+struct BuiltKey {
+    uint64_t handle;
+    uint32_t col;
+    int64_t  dir_bits, radix_bits, dir_cap_bits;
+    bool operator<(const BuiltKey& o) const {
+        return std::tie(handle, col, dir_bits, radix_bits, dir_cap_bits)
+             < std::tie(o.handle, o.col, o.dir_bits, o.radix_bits, o.dir_cap_bits);
+    }
+};
+
+// Tables resident in HBM, shared by a context and the serving slots cloned
+// from it (hj_server); every access holds `mu`.
+struct Store {
+    std::mutex                                  mu;
+    std::map<uint64_t, std::shared_ptr<DevTable>> tables;
+    std::map<BuiltKey, std::shared_ptr<Table>>    built;
+    uint64_t                                    next_handle = 1;
+    int                                         device      = 0;
+    // built tables may be read by kernels on any stream: free them only after
+    // the whole device is idle
+    void drop_built(uint64_t handle) {
+        std::vector<std::shared_ptr<Table>> gone;
+        for (auto it = built.begin(); it != built.end();) {
+            if (it->first.handle == handle || handle == 0) {
+                gone.push_back(it->second);
+                it = built.erase(it);
+            } else {
+                ++it;
+            }
+        }
+        if (gone.empty()) return;
+        cudaSetDevice(device);
+        cudaDeviceSynchronize();
+        for (auto& t : gone) free_table(*t, nullptr);
+        cudaStreamSynchronize(nullptr);
+    }
+    ~Store() { drop_built(0); }
+};
+
 }  // namespace
 }  // namespace hj
 
@@ -214,8 +258,8 @@ struct hj_context {
     size_t              staging_bytes = 0;
     cudaEvent_t         slot_ev[2]  = {nullptr, nullptr};
     std::unique_ptr<hj::ThreadPool>         pool;
-    std::map<uint64_t, std::shared_ptr<hj::DevTable>> resident;
-    uint64_t            next_handle = 1;
+    std::shared_ptr<hj::Store> store;  // resident tables (shared with cloned serving slots)
+    int64_t             table_cache = 0;     // reuse tables built over resident base columns
 };
 
 struct hj_result {
@@ -375,6 +419,8 @@ std::shared_ptr<DevTable> upload_table(hj_context* c, const hj_table_desc& t,
     return dt;
 }
 
+void decode_kernels(cudaStream_t st, DevColumn& d);
+
 // Decodes a device column (idempotent within one execute call); no host
 // synchronisation: sizes come from the page statistics.
 void decode_column(hj_context* c, DevColumn& d, uint32_t table_id, uint32_t col_idx) {
@@ -397,10 +443,15 @@ void decode_column(hj_context* c, DevColumn& d, uint32_t table_id, uint32_t col_
             throw Error(HJ_ERR_OUT_OF_RANGE, "StrRef page overflow: " + std::to_string(d.strref_bad_page)
                                                  + " > " + std::to_string(StrRef::PAGE_MASK));
     }
+    if (d.predecoded) return;  // decoded once when the resident table was prepared
+    decode_kernels(c->st, d);
+}
+
+// The decode kernels of one column (no checks): pages -> plain / tagged / locators.
+void decode_kernels(cudaStream_t st, DevColumn& d) {
     if (d.num_pages == 0 || d.rows == 0) return;
     if (!d.pages) throw Error(HJ_ERR_INVALID, "column pages were not uploaded");
     if (d.type == HJ_INT32 && d.dense1984) return;  // read in place (direct mode)
-    cudaStream_t   st = c->st;
     const uint64_t np = d.num_pages;
     uint32_t*      pr = dalloc_n<uint32_t>(np, st);
     uint64_t*      rs = dalloc_n<uint64_t>(np + 1, st);
@@ -587,7 +638,31 @@ struct Exec {
         int64_t          hint = -1;
         if (bkc.n == 0 || bd.non_null == bd.rows) hint = int64_t(bkc.n);
         else if (!bkc.rid) hint = int64_t(bd.non_null);
-        build_table(bkc, int(c->dir_bits), int(c->radix_bits), t, c->pinned, c->st, hint, int(c->dir_cap_bits));
+        const uint64_t bres = plan.inputs[bk.table].resident;
+        std::shared_ptr<Table> cached;
+        if (c->table_cache && !bkc.rid && bres) {
+            const BuiltKey key{bres, bk.col, c->dir_bits, c->radix_bits, c->dir_cap_bits};
+            {
+                std::lock_guard<std::mutex> g(c->store->mu);
+                auto it = c->store->built.find(key);
+                if (it != c->store->built.end()) cached = it->second;
+            }
+            if (!cached) {
+                auto nt = std::make_shared<Table>();
+                build_table(bkc, int(c->dir_bits), int(c->radix_bits), *nt, c->pinned, c->st, hint,
+                            int(c->dir_cap_bits));
+                // other streams read it from now on: the build must be complete
+                HJ_CUDA(cudaStreamSynchronize(c->st));
+                std::lock_guard<std::mutex> g(c->store->mu);
+                auto ins = c->store->built.emplace(key, nt);
+                if (!ins.second) free_table(*nt, c->st);  // another slot built it meanwhile
+                cached = ins.first->second;
+            }
+            t = *cached;
+        } else {
+            build_table(bkc, int(c->dir_bits), int(c->radix_bits), t, c->pinned, c->st, hint,
+                        int(c->dir_cap_bits));
+        }
         phase("probe");
         ProbeParams prm;
         prm.light_max = int(c->light_max);
@@ -612,11 +687,11 @@ struct Exec {
             if (total > 0) probe_write(t, pkc, pp, ro.data(), int(ro.size()), c->st);
         } catch (...) {
             probe_free(pp, c->st);
-            free_table(t, c->st);
+            if (!cached) free_table(t, c->st);
             throw;
         }
         probe_free(pp, c->st);
-        free_table(t, c->st);
+        if (!cached) free_table(t, c->st);
         out_rows += total;
         return out;
     }
@@ -741,6 +816,32 @@ ProbeParams  context_probe_params(const hj_context* c) {
 void         context_set_error(hj_context* c, const char* msg) { c->err = msg; }
 const Table& hash_table_of(const hj_hash_table* t) { return t->t; }
 
+void result_rebind(hj_result* r, cudaStream_t st) {
+    for (auto& col : r->cols)
+        if (col.pages) col.pages->st = st;
+}
+
+hj_context* context_clone(const hj_context* p) {
+    hj_context* c = hj_context_create(p->device);
+    if (!c) throw Error(HJ_ERR_CUDA, std::string("context for a serving slot: ") + g_create_error);
+    c->store        = p->store;
+    c->dir_bits     = p->dir_bits;
+    c->radix_bits   = p->radix_bits;
+    c->probe_group  = p->probe_group;
+    c->light_max    = p->light_max;
+    c->timing       = p->timing;
+    c->dir_cap_bits = p->dir_cap_bits;
+    c->host_access  = p->host_access;
+    c->table_cache  = p->table_cache;
+    return c;
+}
+
+uint64_t resident_rows(const hj_context* c, uint64_t handle) {
+    std::lock_guard<std::mutex> g(c->store->mu);
+    auto it = c->store->tables.find(handle);
+    return it == c->store->tables.end() ? 0 : it->second->num_rows;
+}
+
 }  // namespace hj
 
 // ===================================================================== C ABI
@@ -776,6 +877,8 @@ hj_context* hj_context_create(int device) {
             pageable = 0;
         }
         c->ats_capable = pageable != 0;
+        c->store         = std::make_shared<hj::Store>();
+        c->store->device = device;
         const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
         c->pool           = std::make_unique<hj::ThreadPool>(std::min(hw, 16u) - 1);
     } catch (const hj::Error& e) {
@@ -789,8 +892,8 @@ hj_context* hj_context_create(int device) {
 void hj_context_destroy(hj_context* c) {
     if (!c) return;
     cudaSetDevice(c->device);
-    c->resident.clear();
     if (c->st) cudaStreamSynchronize(c->st);
+    c->store.reset();  // the last owner frees the resident tables
     for (auto e : c->slot_ev)
         if (e) cudaEventDestroy(e);
     if (c->staging) cudaFreeHost(c->staging);
@@ -822,6 +925,8 @@ int hj_set_option(hj_context* c, const char* name, int64_t v) {
         c->dir_cap_bits = v;
     } else if (n == "host_access") {
         c->host_access = v != 0;
+    } else if (n == "table_cache") {
+        c->table_cache = v != 0;
     } else if (n == "batch_load_pct") {
         if (v < 10 || v > 800) return HJ_ERR_INVALID;
         c->batch_load_pct = v;
@@ -848,6 +953,7 @@ int hj_get_option(const hj_context* c, const char* name, int64_t* v) {
     else if (n == "dir_cap_bits") *v = c->dir_cap_bits;
     else if (n == "host_access") *v = c->host_access;
     else if (n == "host_access_capable") *v = c->ats_capable;
+    else if (n == "table_cache") *v = c->table_cache;
     else if (n == "batch_load_pct") *v = c->batch_load_pct;
     else if (n == "batch_graph") *v = c->batch_graph;
     else if (n == "batch_part_log2") *v = c->batch_part_log2;
@@ -860,16 +966,44 @@ int hj_table_upload(hj_context* c, const hj_table_desc* t, uint64_t* handle) {
     return hj::guarded(c, [&] {
         auto dt = hj::upload_table(c, *t, {});
         HJ_CUDA(cudaStreamSynchronize(c->st));
-        const uint64_t h = c->next_handle++;
-        c->resident[h]   = dt;
+        std::lock_guard<std::mutex> g(c->store->mu);
+        const uint64_t              h = c->store->next_handle++;
+        c->store->tables[h]           = dt;
         *handle          = h;
+    });
+}
+
+int hj_table_prepare(hj_context* c, uint64_t handle) {
+    if (!c) return HJ_ERR_INVALID;
+    return hj::guarded(c, [&] {
+        std::shared_ptr<hj::DevTable> dt;
+        {
+            std::lock_guard<std::mutex> g(c->store->mu);
+            auto it = c->store->tables.find(handle);
+            if (it == c->store->tables.end()) throw hj::Error(HJ_ERR_INVALID, "unknown table handle");
+            dt = it->second;
+        }
+        // decode into a private copy, then publish it: executions that copied
+        // the table meanwhile keep decoding per call
+        auto nt = std::make_shared<hj::DevTable>(*dt);
+        for (auto& col : nt->cols) {
+            if (col.predecoded || (col.type != HJ_INT32 && col.type != HJ_VARCHAR)) continue;
+            hj::decode_kernels(c->st, col);
+            col.predecoded = true;
+        }
+        HJ_CUDA(cudaStreamSynchronize(c->st));
+        std::lock_guard<std::mutex> g(c->store->mu);
+        auto it = c->store->tables.find(handle);
+        if (it != c->store->tables.end()) it->second = nt;
     });
 }
 
 int hj_table_release(hj_context* c, uint64_t handle) {
     if (!c) return HJ_ERR_INVALID;
     return hj::guarded(c, [&] {
-        if (!c->resident.erase(handle)) throw hj::Error(HJ_ERR_INVALID, "unknown table handle");
+        std::lock_guard<std::mutex> g(c->store->mu);
+        if (!c->store->tables.erase(handle)) throw hj::Error(HJ_ERR_INVALID, "unknown table handle");
+        c->store->drop_built(handle);
         HJ_CUDA(cudaStreamSynchronize(c->st));
     });
 }
@@ -904,13 +1038,15 @@ int hj_execute(hj_context* c, const hj_plan_desc* plan, hj_result** out) {
         for (uint32_t i = 0; i < plan->num_inputs; ++i) {
             const hj_table_desc& t = plan->inputs[i];
             if (t.resident) {
-                auto it = c->resident.find(t.resident);
-                if (it == c->resident.end()) throw hj::Error(HJ_ERR_INVALID, "unknown resident table");
-                // decoded state is per call: copy the column records, share the pages
+                std::lock_guard<std::mutex> g(c->store->mu);
+                auto it = c->store->tables.find(t.resident);
+                if (it == c->store->tables.end()) throw hj::Error(HJ_ERR_INVALID, "unknown resident table");
+                // decoded state is per call unless the table was prepared:
+                // copy the column records, share the pages (and decoded arrays)
                 auto dt = std::make_shared<hj::DevTable>(*it->second);
                 for (auto& col : dt->cols) {
                     col.decoded = false;
-                    col.plain = col.tagged = col.locs = nullptr;
+                    if (!col.predecoded) col.plain = col.tagged = col.locs = nullptr;
                 }
                 ex.tables.push_back(dt);
             } else {

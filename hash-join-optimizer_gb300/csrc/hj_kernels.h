@@ -177,10 +177,18 @@ void launch_batch_generate(uint64_t seed, uint32_t instance, uint32_t relation, 
 // Read-only views of C-ABI objects for code outside hj_engine.cu.
 struct hj_context;
 struct hj_hash_table;
+struct hj_result;
 namespace hj {
 int             context_device(const hj_context* c);
 cudaStream_t    context_stream(const hj_context* c);
 ProbeParams     context_probe_params(const hj_context* c);  // options + pinned readback
 void            context_set_error(hj_context* c, const char* msg);
 const Table&    hash_table_of(const hj_hash_table* t);
+// A context on the same device sharing `p`'s resident tables and options (a
+// serving slot: its own stream, pinned buffers and host threads).
+hj_context*     context_clone(const hj_context* p);
+uint64_t        resident_rows(const hj_context* c, uint64_t handle);  // 0 if unknown
+// Frees a result's pages on `st` from now on (the stream it was made on is
+// idle and may go away first).
+void            result_rebind(hj_result* r, cudaStream_t st);
 }  // namespace hj

@@ -129,7 +129,10 @@ void* hj_context_stream(hj_context* ctx);
  * handed to a whole block), "timing" (1: record per-phase device times of
  * each hj_execute, read with hj_result_phase_ms), "host_access" (1, default:
  * where the GPU can read and write pageable host memory, it moves input and
- * result pages itself; 0: host threads stage them through pinned memory).
+ * result pages itself; 0: host threads stage them through pinned memory),
+ * "table_cache" (1: a join whose build side is a whole resident base column
+ * keeps the table built over it in HBM for later plans; 0, default: every
+ * execute builds its own).
  * hj_get_option("host_access_capable") reports whether the device can. */
 int hj_set_option(hj_context* ctx, const char* name, int64_t value);
 int hj_get_option(const hj_context* ctx, const char* name, int64_t* value);
@@ -140,6 +143,10 @@ int hj_get_option(const hj_context* ctx, const char* name, int64_t* value);
  * hj_table_desc.resident.  hj_table_release frees it. */
 int hj_table_upload(hj_context* ctx, const hj_table_desc* table, uint64_t* handle);
 int hj_table_release(hj_context* ctx, uint64_t handle);
+/* Decodes every column of a resident table once and keeps the decoded form in
+ * HBM, so later plans skip the per-call decode (no counterpart in the
+ * reference: its tables are host-resident and decoded per execute). */
+int hj_table_prepare(hj_context* ctx, uint64_t handle);
 
 /* ---- query execution (Contest::execute) ---------------------------------- */
 
@@ -249,6 +256,40 @@ int hj_batch_execute(hj_context* ctx, const hj_batch_instance* instances, uint32
 int hj_batch_generate(hj_context* ctx, uint64_t seed, uint32_t instance, uint32_t relation,
                       uint64_t build_rows, uint32_t match_q24, uint64_t rows, int32_t* keys,
                       int32_t* payload);
+
+/* ---- serving -----------------------------------------------------------------
+ * A request loop over plans.  Clients submit plans from any thread and wait
+ * on tickets; the server runs up to `slots` plans at once, each on its own
+ * CUDA stream and host thread sharing ctx's resident tables (and, with option
+ * "table_cache", the tables built over them), so concurrent plans overlap on
+ * the GPU.  Admission is first come, first served against an HBM budget: a
+ * plan starts when a slot is free and its estimated working memory (tables,
+ * probe lists, row ids and pages, from its inputs' row counts) fits beside the
+ * running ones; one plan larger than the budget runs alone.  Plans read their
+ * inputs while they run: resident handles, or host pages that must stay valid
+ * until the plan's wait returns.  Results are freed with hj_result_free and
+ * read with ctx (hj_result_copy_*).  Destroy the server before ctx; it first
+ * runs the queued plans.  No counterpart in the reference. */
+typedef struct hj_server hj_server;
+typedef struct hj_server_options {
+    uint64_t hbm_budget_bytes; /* working memory of the running plans (estimated) */
+    uint32_t slots;            /* plans running at once, 1..256 */
+} hj_server_options;
+typedef struct hj_request_stats {
+    double   queue_ms;   /* submit -> start */
+    double   service_ms; /* start -> result in HBM */
+    double   latency_ms; /* submit -> result in HBM */
+    uint64_t est_bytes;  /* the admission estimate */
+} hj_request_stats;
+hj_server* hj_server_create(hj_context* ctx, const hj_server_options* opt);
+int        hj_server_submit(hj_server* srv, const hj_plan_desc* plan, uint64_t* ticket);
+/* Blocks until the plan ran; returns its status (message into err when not
+ * NULL) and on success its result. */
+int        hj_server_wait(hj_server* srv, uint64_t ticket, hj_result** out, hj_request_stats* stats,
+                          char* err, uint32_t err_cap);
+int        hj_server_info(hj_server* srv, uint64_t* queued, uint64_t* running, uint64_t* running_bytes,
+                          uint64_t* peak_bytes);
+void       hj_server_destroy(hj_server* srv);
 
 /* ---- host page writers (Table::to_columnar / ColumnInserter packing) ----- */
 

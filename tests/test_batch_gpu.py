@@ -154,3 +154,22 @@ def test_batch_rejects_bad_instances(engine, hj):
     # the context stays usable
     rows, sums, _ = engine.batch_execute([[(k.data_ptr(), k.data_ptr(), 4), (k.data_ptr(), k.data_ptr(), 4)]])
     assert int(rows[0]) == 16
+
+
+def test_autotuner_picks_options_without_changing_results(engine, hj, small_c4, small_c4_truth, tmp_path):
+    from hjgb300 import autotune, batch
+    cache = tmp_path / "tune.json"
+    saved = {k: engine.get_option(k) for k in ("batch_part_log2", "batch_load_pct", "radix_bits", "probe_group")}
+    try:
+        t = autotune.tune(engine, small_c4, sample_instances=24, repeats=1, cache=cache)
+        assert t["batched"]["batch_part_log2"] in autotune.BATCH_PART_LOG2
+        assert t["plain"]["probe_group"] in autotune.PLAIN_PROBE_GROUP
+        assert len(t["sweep"]["batched"]) == len(autotune.BATCH_PART_LOG2) * len(autotune.BATCH_LOAD_PCT)
+        assert autotune.tune(engine, small_c4, cache=cache) == t  # served from the cache
+        autotune.apply(engine, t)
+        for mode in (hj.BATCH_PERSISTENT, hj.BATCH_PLAIN):
+            rows, sums, _, _ = batch.run(engine, small_c4, mode, max_rows=1 << 40)
+            assert np.array_equal(rows, small_c4_truth[0]) and np.array_equal(sums, small_c4_truth[1])
+    finally:
+        for k, v in saved.items():
+            engine.set_option(k, v)

@@ -111,3 +111,28 @@ def test_batch_waves_cover_every_instance(hj):
         assert len(g) == 1 or sum(w.rows(i) for i in g) <= 200_000
     s = w.subset([3, 9])
     assert s.instance(1)[0] == 9 and s.instance(1)[1:] == w.instance(9)[1:]
+
+
+def test_autotune_sample_and_radix_bits(hj):
+    from hjgb300 import autotune, workloads
+    w = workloads.c4(n=500, scale=1.0)
+    s = autotune.sample(w, 64)
+    assert len(s) == 64 and len(set(s.ids.tolist())) == 64
+    # strata cover the size range
+    assert s.build_rows.min() < 2_000 and s.build_rows.max() > 2_000_000
+    assert autotune.radix_bits_for(4000, 12) == 0
+    assert autotune.radix_bits_for(4_000_000, 12) == 10
+    assert autotune.radix_bits_for(12_000_000, 9) == 11  # capped at 11 partition bits
+
+
+def test_serving_schedule_is_a_seeded_poisson_mix(hj):
+    from hjgb300 import serve
+    mix = serve.Mix({"small": [0] * 16, "medium": [0], "large": [0]})
+    a = serve.schedule(mix, rate=1000, n=20_000, seed=1)
+    assert a == serve.schedule(mix, rate=1000, n=20_000, seed=1)
+    t = np.array([x[0] for x in a])
+    assert np.all(np.diff(t) > 0) and abs(t[-1] / 20_000 - 1e-3) < 5e-5       # mean gap 1/rate
+    kinds = np.array([x[1] for x in a])
+    for k, f in zip(serve.KINDS, mix.fractions):
+        assert abs((kinds == k).mean() - f) < 0.015
+    assert {x[2] for x in a if x[1] == "small"} == set(range(16))
