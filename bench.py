@@ -58,6 +58,8 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=2_000_000,
                     help="probe rows of the bounded CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--opt", action="append", default=[], metavar="NAME=VALUE",
+                    help="engine option for the timed runs (hj_set_option), repeatable")
     ap.add_argument("--no-e2e", action="store_true")
     return ap.parse_args()
 
@@ -196,6 +198,9 @@ def run_ours(args, d: Dist) -> dict:
     torch.cuda.set_device(d.local)
     eng = hj.Engine(d.local)
     eng.set_option("timing", 1)
+    for o in args.opt:
+        k, v = o.split("=", 1)
+        eng.set_option(k, int(v))
     w = make_workload(hj, args.workload, args.scale)
     stream = torch.cuda.ExternalStream(eng.stream)
 

@@ -291,7 +291,8 @@ class Result:
     output_rows: int = 0
     phases: dict = field(default_factory=dict)  # device ms per phase (option "timing")
 
-PHASES = ("upload", "decode", "build", "probe", "probe_sync", "probe_write", "materialize", "total", "launches")
+PHASES = ("upload", "decode", "build", "probe", "probe_sync", "probe_write", "materialize", "mat_varchar_plan",
+          "mat_sync", "mat_varchar_write", "total", "launches")
 
 
 class Engine:

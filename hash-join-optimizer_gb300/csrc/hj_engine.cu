@@ -42,20 +42,94 @@ std::atomic<uint64_t> g_kernel_launches{0};
 
 // ---------------------------------------------------------------- memory ----
 
-void* dalloc(size_t bytes, cudaStream_t st) {
-    void* p = nullptr;
-    if (bytes == 0) bytes = 16;
+// Large blocks (result pages, decoded columns, row-id streams: >= 64 MB) are
+// kept per stream when freed and handed back to the next allocation of a
+// similar size on the same stream, without going through the pool: stream
+// order makes the reuse safe, and the host never waits on the pool's memory
+// mapping between two kernels.  flush_stream() returns a stream's blocks.
+namespace {
+constexpr size_t kBig     = size_t(64) << 20;
+constexpr size_t kGranule = size_t(16) << 20;
+struct BigBlocks {
+    std::mutex                                                mu;
+    std::unordered_map<cudaStream_t, std::multimap<size_t, void*>> free;
+    std::unordered_map<void*, size_t>                          size;
+};
+BigBlocks& big_blocks() {
+    static BigBlocks* b = new BigBlocks();  // outlives every context
+    return *b;
+}
+void* pool_alloc(size_t bytes, cudaStream_t st) {
+    void*             p = nullptr;
     const cudaError_t e = cudaMallocAsync(&p, bytes, st);
     if (e != cudaSuccess) {
         cudaGetLastError();
-        throw Error(HJ_ERR_NOMEM, "device allocation of " + std::to_string(bytes) + " bytes failed: "
-                                      + cudaGetErrorString(e));
+        return nullptr;
     }
+    return p;
+}
+}  // namespace
+
+void flush_stream(cudaStream_t st) {
+    BigBlocks&                  b = big_blocks();
+    std::lock_guard<std::mutex> g(b.mu);
+    auto                        it = b.free.find(st);
+    if (it == b.free.end()) return;
+    for (auto& kv : it->second) {
+        b.size.erase(kv.second);
+        cudaFreeAsync(kv.second, st);
+    }
+    b.free.erase(it);
+}
+
+void* dalloc(size_t bytes, cudaStream_t st) {
+    if (bytes == 0) bytes = 16;
+    if (bytes >= kBig) {
+        bytes = (bytes + kGranule - 1) / kGranule * kGranule;
+        BigBlocks& b = big_blocks();
+        {
+            std::lock_guard<std::mutex> g(b.mu);
+            auto&                       m  = b.free[st];
+            auto                        it = m.lower_bound(bytes);
+            if (it != m.end() && it->first <= bytes + bytes / 4) {
+                void* p = it->second;
+                m.erase(it);
+                return p;
+            }
+        }
+        void* p = pool_alloc(bytes, st);
+        if (!p) {  // give every cached block back and try once more
+            std::vector<cudaStream_t> streams;
+            {
+                std::lock_guard<std::mutex> g(b.mu);
+                for (auto& kv : b.free) streams.push_back(kv.first);
+            }
+            for (auto s2 : streams) flush_stream(s2);
+            cudaDeviceSynchronize();
+            p = pool_alloc(bytes, st);
+        }
+        if (!p) throw Error(HJ_ERR_NOMEM, "device allocation of " + std::to_string(bytes) + " bytes failed");
+        std::lock_guard<std::mutex> g(b.mu);
+        b.size[p] = bytes;
+        return p;
+    }
+    void* p = pool_alloc(bytes, st);
+    if (!p) throw Error(HJ_ERR_NOMEM, "device allocation of " + std::to_string(bytes) + " bytes failed");
     return p;
 }
 
 void dfree(void* p, cudaStream_t st) {
-    if (p) cudaFreeAsync(p, st);
+    if (!p) return;
+    {
+        BigBlocks&                  b = big_blocks();
+        std::lock_guard<std::mutex> g(b.mu);
+        auto                        it = b.size.find(p);
+        if (it != b.size.end()) {
+            b.free[st].emplace(it->second, p);
+            return;
+        }
+    }
+    cudaFreeAsync(p, st);
 }
 
 namespace {
@@ -247,7 +321,7 @@ struct hj_context {
     int64_t             probe_group = 8;
     int64_t             light_max   = 32;
     int64_t             timing      = 0;
-    int64_t             dir_cap_bits = 22;  // automatic directories stay <= 32 MB (L2 resident)
+    int64_t             dir_cap_bits = 23;  // automatic directories stay <= 64 MB (L2 resident)
     bool                ats_capable  = false;  // GPU reads/writes pageable host memory
     int64_t             host_access  = 1;      // use it for page transfers when capable
     int64_t             batch_load_pct = 50;   // batched joins: build rows per 100 buckets of a partition table
@@ -710,6 +784,13 @@ struct Exec {
     void materialize(const Inter& in, const hj_node_desc& root, hj_result* res) {
         phase("materialize");
         res->cols.assign(root.num_attrs, hj_result::Col{0, 0, nullptr});
+        struct IntOut {
+            uint32_t        a;
+            IntCol          col;
+            const uint32_t* rid;
+            uint64_t        rows;
+        };
+        std::vector<IntOut>                          iout;  // written after the VARCHAR page counts are known
         std::vector<std::pair<uint32_t, VarcharOut>> vout;  // (column, plan)
         for (uint32_t a = 0; a < root.num_attrs; ++a) {
             const ColRef&   cr  = in.cols[a];
@@ -733,8 +814,8 @@ struct Exec {
                     col.tagged = d.locs->as<uint64_t>();
                 }
                 oc.num_pages = (rows + kDenseRows - 1) / kDenseRows;
-                oc.pages     = make_buf(oc.num_pages * kPage, c->st);
-                launch_write_int32_pages(col, rid, rows, oc.pages->as<uint8_t>(), c->st);
+                oc.pages     = make_buf(oc.num_pages * kPage, c->st);  // allocated while earlier work runs
+                iout.push_back({a, col, rid, rows});
             } else if (ty == HJ_VARCHAR) {
                 VarcharOut v{};
                 if (d.type == HJ_INT32) {
@@ -749,22 +830,30 @@ struct Exec {
                 }
                 v.rid = rid;
                 v.n   = rows;
+                phase("mat_varchar_plan");
                 varchar_plan(v, c->st);
                 vout.emplace_back(a, v);
             }
         }
+        std::vector<uint64_t> vpages;
         if (!vout.empty()) {  // one synchronisation for the page counts of every VARCHAR column
+            phase("mat_sync");
             for (size_t i = 0; i < vout.size(); ++i)
                 HJ_CUDA(cudaMemcpyAsync(c->pinned + i, vout[i].second.tile_off + vout[i].second.ntiles,
                                         sizeof(uint64_t), cudaMemcpyDeviceToHost, c->st));
             HJ_CUDA(cudaStreamSynchronize(c->st));
-            std::vector<uint64_t> pages(c->pinned, c->pinned + vout.size());
-            for (size_t i = 0; i < vout.size(); ++i) {
-                hj_result::Col& oc = res->cols[vout[i].first];
-                oc.num_pages       = pages[i];
-                oc.pages = std::make_shared<DevBuf>(static_cast<void*>(varchar_write(vout[i].second, pages[i], c->st)),
-                                                    c->st);
-            }
+            vpages.assign(c->pinned, c->pinned + vout.size());
+        }
+        // the INT32 pages keep the GPU busy while the host sizes the VARCHAR buffers
+        phase("materialize");
+        for (const IntOut& o : iout)
+            launch_write_int32_pages(o.col, o.rid, o.rows, res->cols[o.a].pages->as<uint8_t>(), c->st);
+        if (!vout.empty()) phase("mat_varchar_write");
+        for (size_t i = 0; i < vout.size(); ++i) {
+            hj_result::Col& oc = res->cols[vout[i].first];
+            oc.num_pages       = vpages[i];
+            oc.pages = std::make_shared<DevBuf>(static_cast<void*>(varchar_write(vout[i].second, vpages[i], c->st)),
+                                                c->st);
         }
         // ColumnarTable::num_rows = rows of the first result column (execute.cpp:437)
         if (root.num_attrs == 0) {
@@ -894,6 +983,10 @@ void hj_context_destroy(hj_context* c) {
     cudaSetDevice(c->device);
     if (c->st) cudaStreamSynchronize(c->st);
     c->store.reset();  // the last owner frees the resident tables
+    if (c->st) {
+        hj::flush_stream(c->st);
+        cudaStreamSynchronize(c->st);
+    }
     for (auto e : c->slot_ev)
         if (e) cudaEventDestroy(e);
     if (c->staging) cudaFreeHost(c->staging);

@@ -13,9 +13,11 @@
 namespace hj {
 
 // Stream-ordered device memory (cudaMallocAsync on a pool that keeps freed
-// blocks cached for reuse).
+// blocks cached for reuse; blocks of 64 MB and more are reused per stream).
 void* dalloc(size_t bytes, cudaStream_t st);
 void  dfree(void* p, cudaStream_t st);
+// Returns the large blocks kept for reuse on `st` (before `st` is destroyed).
+void  flush_stream(cudaStream_t st);
 
 template <class T>
 T* dalloc_n(size_t n, cudaStream_t st) {

@@ -341,6 +341,7 @@ uint8_t* varchar_write(VarcharOut& v, uint64_t pages, cudaStream_t st) {
                                                            desc);
     HJ_LAUNCH_CHECK();
     auto* out = static_cast<uint8_t*>(dalloc(std::max<uint64_t>(pages, 1) * kPage, st));
+
     k_write_varchar_pages<<<grid_of(pages), kMT, 0, st>>>(desc, pages, v.ol, v.base, v.base_pages, out);
     HJ_LAUNCH_CHECK();
     for (void* p : {(void*)desc, (void*)v.ol, (void*)v.tile_pages, (void*)v.tile_off}) dfree(p, st);
