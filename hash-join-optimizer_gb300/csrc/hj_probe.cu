@@ -207,6 +207,12 @@ __global__ void __launch_bounds__(kPT)
     }
 }
 
+// Grid of the count pass: up to 8 blocks of 256 threads per SM, looping over
+// the tiles (measured faster than a register-capped single resident wave).
+int probe_count_grid(uint64_t ntiles) {
+    return int(std::max<uint64_t>(1, std::min<uint64_t>(ntiles, uint64_t(kSMs) * 8)));
+}
+
 __global__ void __launch_bounds__(512) k_mixed_count(ProbeTab T, Lists Ls) {
     __shared__ unsigned long long s_red[33];
     const uint64_t n   = Ls.ctr[2];
@@ -389,7 +395,7 @@ uint64_t probe_count(const Table& t, const KeyCol& pk, const ProbeParams& prm, P
     HJ_CUDA(cudaMemsetAsync(L.ctr, 0, 8 * sizeof(unsigned long long), st));
     const ProbeTab T      = tab_of(t);
     const uint64_t ntiles = (n + kPTile - 1) / kPTile;
-    const int      grid   = int(std::min<uint64_t>(ntiles, uint64_t(kSMs) * 8));
+    const int      grid   = probe_count_grid(ntiles);
     k_probe_count<<<grid, kPT, 0, st>>>(T, pk, prm.light_max, L, ntiles);
     HJ_LAUNCH_CHECK();
     k_mixed_count<<<kSMs * 2, 512, 0, st>>>(T, L);
@@ -516,7 +522,7 @@ int probe_into_scratch(const Table& t, const KeyCol& pk, const ProbeParams& prm,
     HJ_CUDA(cudaMemsetAsync(L.ctr, 0, 8 * sizeof(unsigned long long), st));
     const ProbeTab T      = tab_of(t);
     const uint64_t ntiles = (n + kPTile - 1) / kPTile;
-    const int      grid   = int(std::min<uint64_t>(ntiles, uint64_t(kSMs) * 8));
+    const int      grid   = probe_count_grid(ntiles);
     k_probe_count<<<grid, kPT, 0, st>>>(T, pk, prm.light_max, L, ntiles);
     HJ_LAUNCH_CHECK();
     k_mixed_count<<<kSMs * 2, 512, 0, st>>>(T, L);
