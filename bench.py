@@ -44,7 +44,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["c1", "c2", "c3", "c4", "c5"], default="c2")
+    ap.add_argument("--workload", choices=["c1", "c2", "c2raw", "c3", "c4", "c5"], default="c2")
     ap.add_argument("--rates", default="50,100,200,500,1000,2000,5000", help="c5: offered queries/s")
     ap.add_argument("--requests", type=int, default=200, help="c5: requests per rate")
     ap.add_argument("--slots", type=int, default=8, help="c5: plans running at once")

@@ -19,6 +19,8 @@ import numpy as np
 PAGE_SIZE = 8192
 INT32, INT64, FP64, VARCHAR = 0, 1, 2, 3
 NODE_JOIN, NODE_SCAN = 0, 1
+# scan filter operators (Comparison::Op numbering)
+CMP_EQ, CMP_NEQ, CMP_LT, CMP_GT, CMP_LEQ, CMP_GEQ, CMP_IS_NULL, CMP_IS_NOT_NULL = 0, 1, 2, 3, 4, 5, 8, 9
 
 HJ_OK, HJ_ERR_INVALID, HJ_ERR_RUNTIME, HJ_ERR_OUT_OF_RANGE = 0, 1, 2, 3
 HJ_ERR_CUDA, HJ_ERR_NO_DEVICE, HJ_ERR_CAPACITY, HJ_ERR_DEVICE_STATUS, HJ_ERR_NOMEM = 4, 5, 6, 7, 8
@@ -63,10 +65,15 @@ class Attr(C.Structure):
     _fields_ = [("index", C.c_uint64), ("type", C.c_int32)]
 
 
+class FilterDesc(C.Structure):
+    _fields_ = [("column", C.c_uint64), ("op", C.c_int32), ("pad", C.c_int32), ("value", C.c_int64)]
+
+
 class NodeDesc(C.Structure):
     _fields_ = [("kind", C.c_int32), ("build_left", C.c_int32), ("base_table_id", C.c_uint64),
                 ("left", C.c_uint64), ("right", C.c_uint64), ("left_attr", C.c_uint64),
-                ("right_attr", C.c_uint64), ("num_attrs", C.c_uint32), ("attrs", C.POINTER(Attr))]
+                ("right_attr", C.c_uint64), ("num_attrs", C.c_uint32), ("attrs", C.POINTER(Attr)),
+                ("num_filters", C.c_uint32), ("filters", C.POINTER(FilterDesc))]
 
 
 class PlanDesc(C.Structure):
@@ -214,8 +221,14 @@ class Plan:
     inputs: list = field(default_factory=list)
     root: int = 0
 
-    def new_scan_node(self, base_table_id: int, output_attrs: Sequence[tuple]) -> int:
-        self.nodes.append(("scan", int(base_table_id), [(int(i), int(t)) for i, t in output_attrs]))
+    def new_scan_node(self, base_table_id: int, output_attrs: Sequence[tuple],
+                      filters: Sequence[tuple] = ()) -> int:
+        """filters: (column, CMP_* operator, int literal) triples, AND-combined, on INT32
+        columns of the table (the reference applies them while loading the table)."""
+        node = ("scan", int(base_table_id), [(int(i), int(t)) for i, t in output_attrs])
+        if filters:
+            node = node + ([(int(c), int(o), int(v)) for c, o, v in filters],)
+        self.nodes.append(node)
         return len(self.nodes) - 1
 
     def new_join_node(self, build_left: bool, left: int, right: int, left_attr: int, right_attr: int,
@@ -232,13 +245,18 @@ class Plan:
         """(PlanDesc, keepalive) for the C ABI; keepalive must outlive the call."""
         keep = []
         nodes = (NodeDesc * max(1, len(self.nodes)))()
-        for i, (kind, data, attrs) in enumerate(self.nodes):
+        for i, node in enumerate(self.nodes):
+            kind, data, attrs = node[:3]
             arr = (Attr * max(1, len(attrs)))(*[Attr(a, t) for a, t in attrs])
             keep.append(arr)
             nd = nodes[i]
             nd.num_attrs, nd.attrs = len(attrs), arr
             if kind == "scan":
                 nd.kind, nd.base_table_id = NODE_SCAN, data
+                if len(node) > 3:
+                    fl = (FilterDesc * len(node[3]))(*[FilterDesc(c, o, 0, v) for c, o, v in node[3]])
+                    keep.append(fl)
+                    nd.num_filters, nd.filters = len(node[3]), fl
             else:
                 nd.kind = NODE_JOIN
                 nd.build_left, nd.left, nd.right, nd.left_attr, nd.right_attr = int(data[0]), *data[1:]

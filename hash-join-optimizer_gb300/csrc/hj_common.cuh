@@ -97,6 +97,41 @@ __device__ __forceinline__ bool int_get(const IntCol& c, uint64_t r, int32_t& v)
     return true;
 }
 
+// Scan predicates (hj_filter) over INT32 base columns, AND-combined.
+constexpr int kMaxFilters = HJ_MAX_SCAN_FILTERS;
+struct Filt {
+    IntCol  col;
+    int32_t op;
+    int32_t val;
+};
+struct Filters {
+    int  n = 0;
+    Filt f[kMaxFilters];
+};
+
+// Does base row r pass every filter?  NULL never compares true; IS_NULL /
+// IS_NOT_NULL test validity (the reference's bitmap & comparison).
+__device__ __forceinline__ bool filt_pass(const Filters& F, uint64_t r) {
+    for (int i = 0; i < F.n; ++i) {
+        int32_t    v     = 0;
+        const bool valid = int_get(F.f[i].col, r, v);
+        const int32_t x  = F.f[i].val;
+        bool          ok;
+        switch (F.f[i].op) {
+            case HJ_CMP_EQ: ok = valid && v == x; break;
+            case HJ_CMP_NEQ: ok = valid && v != x; break;
+            case HJ_CMP_LT: ok = valid && v < x; break;
+            case HJ_CMP_GT: ok = valid && v > x; break;
+            case HJ_CMP_LEQ: ok = valid && v <= x; break;
+            case HJ_CMP_GEQ: ok = valid && v >= x; break;
+            case HJ_CMP_IS_NULL: ok = !valid; break;
+            default: ok = valid; break;  // HJ_CMP_IS_NOT_NULL
+        }
+        if (!ok) return false;
+    }
+    return true;
+}
+
 // A VARCHAR base column is decoded to one 64-bit locator per row: 0 = NULL;
 // otherwise bit 63 set, bit 62 = long string (0xffff page + 0xfffe pages),
 // bits 40..61 = byte length (saturated at 2^22 - 1 for long strings, whose

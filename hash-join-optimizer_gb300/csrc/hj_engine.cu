@@ -562,6 +562,7 @@ struct Inter {
     uint64_t               rows = 0;
     std::vector<Source>    srcs;
     std::vector<ColRef>    cols;
+    Filters                filt;  // a scan's predicates not yet applied (rows = the table's rows)
 };
 
 struct Exec {
@@ -629,7 +630,35 @@ struct Exec {
                                                 + std::to_string(n.attrs[a].index) + ")");
             common = int64_t(d.rows);
         }
+        // scan predicates: applied later, fused into a probe or by compaction
+        if (n.num_filters > 0) {
+            if (n.num_filters > uint32_t(kMaxFilters) || !n.filters)
+                throw Error(HJ_ERR_INVALID, "at most " + std::to_string(kMaxFilters) + " filters per scan");
+            for (uint32_t i = 0; i < n.num_filters; ++i) {
+                const hj_filter& f = n.filters[i];
+                if (f.column >= tables[t]->cols.size()) throw Error(HJ_ERR_INVALID, "filter column out of range");
+                const DevColumn& d = column(t, uint32_t(f.column));
+                if (d.type != HJ_INT32) throw Error(HJ_ERR_INVALID, "filter column is not INT32");
+                if (d.rows != in.rows)
+                    throw Error(HJ_ERR_INVALID, "filter column of input table " + std::to_string(t)
+                                                    + " has a different row count");
+                const bool op_ok = (f.op >= HJ_CMP_EQ && f.op <= HJ_CMP_GEQ) || f.op == HJ_CMP_IS_NULL
+                                || f.op == HJ_CMP_IS_NOT_NULL;
+                if (!op_ok) throw Error(HJ_ERR_INVALID, "unsupported filter operator " + std::to_string(f.op));
+                // the literal is cast as Comparison::eval does (src/statement.cpp:56)
+                in.filt.f[in.filt.n++] = Filt{d.icol(), f.op, static_cast<int32_t>(f.value)};
+            }
+        }
         return in;
+    }
+
+    // Applies a scan's pending predicates: its passing rows become row ids, in order.
+    void compact(Inter& in) {
+        if (in.filt.n == 0) return;
+        Buf rid = make_buf(std::max<uint64_t>(in.rows, 1) * 4, c->st);
+        in.rows = filter_compact(in.filt, in.rows, rid->as<uint32_t>(), c->pinned, c->st);
+        in.srcs[0].rid = rid;
+        in.filt.n      = 0;
     }
 
     // Number of non-NULL rows of a column seen through a source's row ids.
@@ -676,10 +705,14 @@ struct Exec {
         if (battr >= B.cols.size() || pattr >= P.cols.size())
             throw Error(HJ_ERR_INVALID, "join attribute out of range");
         const ColRef bk = B.cols[battr], pk = P.cols[pattr];
+        // A filtered build side is compacted; a filtered probe side is read raw
+        // and its predicate evaluated by the probe's count pass.
+        compact(B);
         // Non-INT32 join keys: the reference throws on the first non-NULL value
         // (execute.cpp:81,130).
         for (auto [in, cr] : {std::pair<Inter*, ColRef>{&B, bk}, std::pair<Inter*, ColRef>{&P, pk}}) {
             DevColumn& d = column(cr.table, cr.col);
+            if (d.type == HJ_VARCHAR) compact(*in);
             if (d.type == HJ_VARCHAR && non_null_through(*in, cr) > 0)
                 throw Error(HJ_ERR_RUNTIME, "Join key isn't of type int32_t");
         }
@@ -702,6 +735,7 @@ struct Exec {
             out.cols.push_back(ColRef{src_slot(is_b ? 1 : 0, cr.src), cr.table, cr.col});
         }
         KeyCol bkc = key_col(B, bk), pkc = key_col(P, pk);
+        pkc.filt   = P.filt;  // fused scan predicate (raw rows, no row ids)
         build_tuples += bkc.n;
         probe_tuples += pkc.n;
         Table t;
@@ -1126,6 +1160,8 @@ int hj_execute(hj_context* c, const hj_plan_desc* plan, hj_result** out) {
                 if (col >= t.num_columns) throw hj::Error(HJ_ERR_INVALID, "scan column out of range");
                 want[n.base_table_id][col] = true;
             }
+            for (uint32_t f = 0; f < n.num_filters && n.filters && !t.resident; ++f)
+                if (n.filters[f].column < t.num_columns) want[n.base_table_id][n.filters[f].column] = true;
         }
         ex.phase("upload");
         for (uint32_t i = 0; i < plan->num_inputs; ++i) {
@@ -1156,8 +1192,12 @@ int hj_execute(hj_context* c, const hj_plan_desc* plan, hj_result** out) {
                     throw hj::Error(HJ_ERR_INVALID, "scan column out of range");
                 ex.column(uint32_t(n.base_table_id), uint32_t(n.attrs[a].index));
             }
+            for (uint32_t f = 0; f < n.num_filters && n.filters; ++f)
+                if (n.filters[f].column < ex.tables[n.base_table_id]->cols.size())
+                    ex.column(uint32_t(n.base_table_id), uint32_t(n.filters[f].column));
         }
         hj::Inter root = ex.run(plan->root);
+        ex.compact(root);  // a filtered scan as the root
         ex.materialize(root, plan->nodes[plan->root], res);
         ex.collect(res->phase_ms);
         HJ_CUDA(cudaStreamSynchronize(c->st));

@@ -61,7 +61,13 @@ struct KeyCol {
     IntCol          col;    // the base column
     const uint32_t* rid;    // row ids into the base column, or nullptr = identity
     uint64_t        n;      // rows of the (intermediate) column
+    Filters         filt;   // probe side only: scan predicates evaluated on base row ids (rid == nullptr)
 };
+
+// ---- scan predicates (hj_filter.cu) ----------------------------------------
+// Base rows 0..n-1 that pass `f`, in order, into rid_out (n slots); returns their
+// number (one host synchronisation through `pinned`).
+uint64_t filter_compact(const Filters& f, uint64_t n, uint32_t* rid_out, uint64_t* pinned, cudaStream_t st);
 
 struct Table {
     uint32_t  dir_bits  = 0;

@@ -90,7 +90,12 @@ __global__ void __launch_bounds__(kPT)
             const uint64_t j = tile * kPTile + uint64_t(it) * kPT + threadIdx.x;
             ok[it]           = false;
             key[it]          = 0;
-            if (j < pk.n) ok[it] = int_get(pk.col, pk.rid ? uint64_t(__ldg(pk.rid + j)) : j, key[it]);
+            if (j < pk.n) {
+                const uint64_t row = pk.rid ? uint64_t(__ldg(pk.rid + j)) : j;
+                ok[it]             = int_get(pk.col, row, key[it]);
+                // a filtered scan read raw: rows failing its predicate never match
+                if (pk.filt.n && ok[it]) ok[it] = filt_pass(pk.filt, row);
+            }
         }
 #pragma unroll
         for (int it = 0; it < kPI; ++it) {

@@ -30,7 +30,7 @@ from typing import Callable, Optional
 
 import numpy as np
 
-from . import INT32, VARCHAR, Column, Plan, Table
+from . import CMP_LT, INT32, VARCHAR, Column, Plan, Table
 
 
 @dataclass
@@ -96,7 +96,12 @@ def c1(scale: float = 1.0, seed: int = 42) -> Workload:
                     sample=lambda k: make_plan(min(k, npr)))
 
 
-def c2(scale: float = 1.0, seed: int = 42, raw_probe: int | None = None) -> Workload:
+def c2(scale: float = 1.0, seed: int = 42, raw_probe: int | None = None, raw: bool = False) -> Workload:
+    """raw=True: the probe side is the raw table (all probe rows plus the
+    predicate column `pred`, column 4) and the plan's probe scan carries the
+    predicate pred < 100 instead of the table being pre-filtered.  Its passing
+    rows hold exactly the pre-filtered table's values, so the result is the
+    same; dropped rows get their own random keys and payloads and NULL strings."""
     nb = max(1, int(16_000_000 * scale))
     kb, kp = max(1, int(4_000_000 * scale)), max(1, int(8_000_000 * scale))
     nraw = raw_probe if raw_probe is not None else max(1, int(256_000_000 * scale))
@@ -108,7 +113,8 @@ def c2(scale: float = 1.0, seed: int = 42, raw_probe: int | None = None) -> Work
     v1, v2 = nulls(rb, nb, 0.2), nulls(rb, nb, 0.2)
     bs, bo = ascii_strings(rb, nb, 8, 64)
     # pre-filter: pred ~ U[0, 1000) over the raw probe rows, keep pred < 100
-    keep = np.flatnonzero(rp.integers(0, 1000, size=nraw, dtype=np.int16) < 100)
+    pred = rp.integers(0, 1000, size=nraw, dtype=np.int16)
+    keep = np.flatnonzero(pred < 100)
     npr = int(keep.size)
     perm_p = rp.permutation(kp).astype(np.int32)
     fk = perm_p[zipf_ranks(rp, npr, kp, 1.1)]
@@ -137,6 +143,38 @@ def c2(scale: float = 1.0, seed: int = 42, raw_probe: int | None = None) -> Work
                                                           (5, INT32), (6, INT32), (7, VARCHAR)])
         return plan
 
+    if raw:
+        rr = _rng(seed, 2, 2)
+        drop = np.ones(nraw, dtype=bool)
+        drop[keep] = False
+
+        def spread(kept, fill):
+            out = np.empty(nraw, dtype=kept.dtype)
+            out[keep] = kept
+            out[drop] = fill
+            return out
+        nd = int(drop.sum())
+        fk_r = spread(fk, rr.integers(0, kp, size=nd, dtype=np.int64).astype(np.int32))
+        p1_r = spread(p1, rr.integers(0, 2**31, size=nd, dtype=np.int64).astype(np.int32))
+        p2_r = spread(p2, rr.integers(0, 2**31, size=nd, dtype=np.int64).astype(np.int32))
+        w1_r, w2_r = spread(w1, nulls(rr, nd, 0.2)), spread(w2, nulls(rr, nd, 0.2))
+        lens = np.zeros(nraw, dtype=np.int64)
+        lens[keep] = np.diff(po.astype(np.int64))
+        po_r = np.zeros(nraw + 1, dtype=np.uint64)
+        np.cumsum(lens, out=po_r[1:])
+        vs_r = (~drop).astype(np.uint8)
+        raw_probe_t = Table(nraw, [Column.int32(fk_r), Column.int32(p1_r, w1_r), Column.int32(p2_r, w2_r),
+                                   Column.varchar(ps, po_r, vs_r), Column.int32(pred.astype(np.int32))])
+        plan = Plan()
+        plan.new_input(build)
+        plan.new_input(raw_probe_t)
+        plan.new_scan_node(0, [(0, INT32), (1, INT32), (2, INT32), (3, VARCHAR)])
+        plan.new_scan_node(1, [(0, INT32), (1, INT32), (2, INT32), (3, VARCHAR)], filters=[(4, CMP_LT, 100)])
+        plan.root = plan.new_join_node(True, 0, 1, 0, 0, [(1, INT32), (2, INT32), (3, VARCHAR),
+                                                          (5, INT32), (6, INT32), (7, VARCHAR)])
+        return Workload("c2raw", plan, nraw, nb, expected_rows=expected,
+                        meta={"build_rows": nb, "probe_rows_raw": nraw, "probe_rows": npr,
+                              "prefiltered_plan": make_plan(probe_table(npr))})
     return Workload("c2", make_plan(probe_table(npr)), npr, nb, expected_rows=expected,
                     meta={"build_rows": nb, "probe_rows_raw": nraw, "probe_rows": npr,
                           "build_key_domain": kb, "probe_key_domain": kp,
@@ -145,6 +183,11 @@ def c2(scale: float = 1.0, seed: int = 42, raw_probe: int | None = None) -> Work
 
 
 C3_SIZES = (36_000_000, 15_000_000, 4_200_000, 2_500_000, 134_000)
+
+
+def c2raw(scale: float = 1.0, seed: int = 42) -> Workload:
+    """c2 with the predicate fused into the probe: the raw probe table and a scan filter."""
+    return c2(scale, seed, raw=True)
 
 
 def c3(scale: float = 1.0, seed: int = 42) -> Workload:

@@ -82,16 +82,41 @@ typedef struct hj_attr {
 
 /* PlanNode.  kind = HJ_NODE_SCAN uses base_table_id; kind = HJ_NODE_JOIN uses
  * build_left/left/right/left_attr/right_attr with the meaning of JoinNode. */
+/* A scan predicate on an INT32 column of the scanned table: the reference's
+ * Comparison (include/statement.h:53-184 with src/statement.cpp:46-67 and
+ * include/inner_column.h:172-326), which its table loader applies before
+ * execute() (src/build_table.cpp:321-325).  A row passes when its bitmap bit is
+ * set and `value OP literal` holds (a NULL never compares true); IS_NULL /
+ * IS_NOT_NULL test the bitmap; the literal is cast to int32 as the reference
+ * does.  The filters of one scan are combined with AND (LogicalOperation AND).
+ * Operator numbers follow Comparison::Op; LIKE / NOT LIKE are not INT32
+ * operators and are rejected. */
+enum { HJ_CMP_EQ = 0, HJ_CMP_NEQ = 1, HJ_CMP_LT = 2, HJ_CMP_GT = 3, HJ_CMP_LEQ = 4, HJ_CMP_GEQ = 5,
+       HJ_CMP_IS_NULL = 8, HJ_CMP_IS_NOT_NULL = 9 };
+#define HJ_MAX_SCAN_FILTERS 4
+typedef struct hj_filter {
+    uint64_t column; /* column index in the scanned table */
+    int32_t  op;     /* HJ_CMP_* */
+    int32_t  pad;
+    int64_t  value;  /* the literal */
+} hj_filter;
+
 typedef struct hj_node_desc {
-    int32_t        kind;
-    int32_t        build_left;
-    uint64_t       base_table_id;
-    uint64_t       left;
-    uint64_t       right;
-    uint64_t       left_attr;
-    uint64_t       right_attr;
-    uint32_t       num_attrs;
-    const hj_attr* attrs;
+    int32_t          kind;
+    int32_t          build_left;
+    uint64_t         base_table_id;
+    uint64_t         left;
+    uint64_t         right;
+    uint64_t         left_attr;
+    uint64_t         right_attr;
+    uint32_t         num_attrs;
+    const hj_attr*   attrs;
+    /* scan nodes only: rows of the base table that pass all filters (none = all
+     * rows).  A filtered scan on the probe side of a join is evaluated inside
+     * the probe's first pass over the raw rows; elsewhere its passing rows are
+     * compacted in order. */
+    uint32_t         num_filters;
+    const hj_filter* filters;
 } hj_node_desc;
 
 typedef struct hj_plan_desc {

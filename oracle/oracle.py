@@ -64,8 +64,7 @@ def port() -> C.CDLL:
     global _port
     if _port is None:
         so = HERE / "liboracle.so"
-        if not so.exists():
-            build(with_ref=False)
+        build(with_ref=False)  # make: rebuilds when a source or include/hj_api.h changed
         L = _setup(C.CDLL(str(so)), "oracle_execute")
         vp, u64 = C.c_void_p, C.c_uint64
         L.oracle_decode_int32.argtypes = [vp, u64, vp, vp, u64, C.POINTER(u64)]
@@ -84,10 +83,10 @@ def ref() -> Optional[C.CDLL]:
     global _ref
     if _ref is None:
         so = HERE / "_ref" / "libhjref.so"
-        if not so.exists():
-            if not Path(os.environ.get("HJ_REFERENCE", "/root/reference"), "src").is_dir():
-                return None
-            build(with_ref=True)
+        if Path(os.environ.get("HJ_REFERENCE", "/root/reference"), "src").is_dir():
+            build(with_ref=True)  # make: rebuilds when a source or include/hj_api.h changed
+        elif not so.exists():
+            return None
         try:
             L = _setup(C.CDLL(str(so)), "ref_execute")
         except OSError:  # built for another architecture

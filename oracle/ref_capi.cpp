@@ -50,6 +50,7 @@ Plan to_plan(const hj_plan_desc& d) {
     Plan plan;
     for (uint32_t i = 0; i < d.num_nodes; ++i) {
         const hj_node_desc& n = d.nodes[i];
+        if (n.num_filters) throw std::invalid_argument("the reference's Plan has no scan filters");
         std::vector<std::tuple<size_t, DataType>> attrs;
         for (uint32_t a = 0; a < n.num_attrs; ++a)
             attrs.emplace_back(size_t(n.attrs[a].index), static_cast<DataType>(n.attrs[a].type));

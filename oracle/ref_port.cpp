@@ -350,6 +350,9 @@ Result hash_join(bool build_left, Result& left, Result& right, size_t left_attr,
 
 Result execute_impl(const hj_plan_desc& plan, size_t node) {
     const hj_node_desc& n = plan.nodes[node];
+    // execute() receives tables already filtered by the loader; scan filters
+    // have no counterpart here (tests compare them with pre-filtered plans)
+    if (n.num_filters) throw std::invalid_argument("the oracle takes no scan filters");
     if (n.kind == HJ_NODE_SCAN)
         return copy_scan(plan.inputs[n.base_table_id], n.base_table_id, n.attrs, n.num_attrs);
     Result left  = execute_impl(plan, n.left);

@@ -7,6 +7,7 @@ import re
 import subprocess
 from pathlib import Path
 
+import numpy as np
 import pytest
 
 ROOT = Path(__file__).resolve().parents[1]
@@ -75,3 +76,16 @@ def test_invalid_arguments_are_rejected_without_gpu(hj):
     assert lib.hj_set_option(None, b"dir_bits", 3) == hj.HJ_ERR_INVALID
     n = C.c_uint64()
     assert lib.hj_pages_from_int32(None, None, 5, None, 0, C.byref(n)) == hj.HJ_ERR_INVALID
+
+
+def test_scan_filters_reach_the_c_abi_and_the_oracle_refuses_them(hj, orc):
+    import ctypes as C
+    p = hj.Plan()
+    p.new_input(hj.Table(3, [hj.Column.int32(np.array([1, 2, 3], np.int32))]))
+    p.root = p.new_scan_node(0, [(0, hj.INT32)], filters=[(0, hj.CMP_GEQ, 2), (0, hj.CMP_IS_NOT_NULL, 0)])
+    d, keep = p.desc()
+    n = d.nodes[0]
+    assert n.num_filters == 2 and n.filters[0].op == hj.CMP_GEQ and n.filters[0].value == 2
+    assert C.sizeof(hj.FilterDesc) == 24
+    out = orc.run(orc.port(), p)
+    assert out.status != 0 and "filter" in out.error
