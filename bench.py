@@ -269,8 +269,15 @@ def run_ours(args, d: Dist) -> dict:
         h2d = sum(c.num_pages for t in w.plan.inputs for c in t.columns) * hj.PAGE_SIZE
         d2h_seen = []
 
+        e2e_parts = {"upload_ms": 0.0, "execute_ms": 0.0, "fetch_ms": 0.0}
+
         def e2e_step():
+            t0 = time.perf_counter()
             r = eng.execute_raw(w.plan)
+            t1 = time.perf_counter()
+            ph = eng.stats(r)[3]
+            e2e_parts["upload_ms"] += ph.get("upload", 0.0)
+            e2e_parts["execute_ms"] += 1e3 * (t1 - t0) - ph.get("upload", 0.0)
             total = 0
             for i in range(len(host_bufs)):
                 ty, npg = C.c_int32(), C.c_uint64()
@@ -281,9 +288,12 @@ def run_ours(args, d: Dist) -> dict:
                     assert L.hj_result_copy_contiguous(eng.handle, r, i, host_bufs[i].ctypes.data) == 0
                 total += npg.value
             d2h_seen.append(total * hj.PAGE_SIZE)
+            e2e_parts["fetch_ms"] += 1e3 * (time.perf_counter() - t1)
             eng.free_result(r)
 
         e2e_step()
+        for k in e2e_parts:
+            e2e_parts[k] = 0.0
         d.barrier()
         torch.cuda.synchronize()
         s2, e2 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -295,7 +305,8 @@ def run_ours(args, d: Dist) -> dict:
         torch.cuda.synchronize()
         ms2 = d.max(s2.elapsed_time(e2) / k2)
         e2e = {"value": npr * d.world / (ms2 / 1e3), "unit": "probe tuples/s", "ms_per_step": ms2,
-               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": int(sum(d2h_seen[1:]) / max(1, len(d2h_seen) - 1))}
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": int(sum(d2h_seen[1:]) / max(1, len(d2h_seen) - 1)),
+               "parts_ms": {k: round(v / k2, 3) for k, v in e2e_parts.items()}}
 
     # ---- CPU baseline (rank 0, bounded sample)
     cpu = None

@@ -864,10 +864,14 @@ struct Exec {
                 }
                 v.rid = rid;
                 v.n   = rows;
-                phase("mat_varchar_plan");
-                varchar_plan(v, c->st);
                 vout.emplace_back(a, v);
             }
+        }
+        std::vector<VarcharOut*> vptr;
+        for (auto& kv : vout) vptr.push_back(&kv.second);
+        if (!vout.empty()) {
+            phase("mat_varchar_plan");
+            varchar_plan(vptr, c->st);
         }
         std::vector<uint64_t> vpages;
         if (!vout.empty()) {  // one synchronisation for the page counts of every VARCHAR column
@@ -882,12 +886,14 @@ struct Exec {
         phase("materialize");
         for (const IntOut& o : iout)
             launch_write_int32_pages(o.col, o.rid, o.rows, res->cols[o.a].pages->as<uint8_t>(), c->st);
-        if (!vout.empty()) phase("mat_varchar_write");
-        for (size_t i = 0; i < vout.size(); ++i) {
-            hj_result::Col& oc = res->cols[vout[i].first];
-            oc.num_pages       = vpages[i];
-            oc.pages = std::make_shared<DevBuf>(static_cast<void*>(varchar_write(vout[i].second, vpages[i], c->st)),
-                                                c->st);
+        if (!vout.empty()) {
+            phase("mat_varchar_write");
+            const std::vector<uint8_t*> bufs = varchar_write(vptr, vpages, c->st);
+            for (size_t i = 0; i < vout.size(); ++i) {
+                hj_result::Col& oc = res->cols[vout[i].first];
+                oc.num_pages       = vpages[i];
+                oc.pages           = std::make_shared<DevBuf>(static_cast<void*>(bufs[i]), c->st);
+            }
         }
         // ColumnarTable::num_rows = rows of the first result column (execute.cpp:437)
         if (root.num_attrs == 0) {

@@ -132,6 +132,8 @@ int    probe_into_scratch(const Table& t, const KeyCol& pk, const ProbeParams& p
 void launch_write_int32_pages(const IntCol& col, const uint32_t* rid, uint64_t n, uint8_t* out_pages,
                               cudaStream_t st);
 
+struct PageDesc;  // one output page of a VARCHAR column (hj_materialize.cu)
+
 // VARCHAR output columns in two steps, so that several columns share one
 // host synchronisation: plan (gather locators, pack pages, count them into
 // *page_count, a device word) then write (after the caller read the counts).
@@ -142,14 +144,17 @@ struct VarcharOut {
     const uint32_t* rid;         // row ids or nullptr
     uint64_t        n;           // output rows
     // filled by varchar_plan
-    uint64_t* ol         = nullptr;  // gathered locators, n
-    uint32_t* tile_pages = nullptr;
-    uint64_t* tile_off   = nullptr;  // ntiles + 1 (last = page count, on the device)
-    uint64_t  ntiles     = 0;
+    uint64_t*       ol         = nullptr;  // gathered locators, n
+    uint32_t*       tile_pages = nullptr;
+    uint64_t*       tile_off   = nullptr;  // ntiles + 1 (last = page count, on the device)
+    uint64_t        ntiles     = 0;
+    PageDesc*       desc       = nullptr;  // varchar_write's page descriptors
 };
-void     varchar_plan(VarcharOut& v, cudaStream_t st);
-// pages = tile_off[ntiles] as read by the caller; returns the page buffer.
-uint8_t* varchar_write(VarcharOut& v, uint64_t pages, cudaStream_t st);
+// All VARCHAR columns of a result at once (their packing kernels share launches).
+void varchar_plan(std::vector<VarcharOut*>& vs, cudaStream_t st);
+// pages[i] = vs[i]->tile_off[ntiles] as read by the caller; returns the page buffers.
+std::vector<uint8_t*> varchar_write(std::vector<VarcharOut*>& vs, const std::vector<uint64_t>& pages,
+                                    cudaStream_t st);
 
 // ---- batched independent joins (hj_batch.cu) ------------------------------
 // One relation of a batch instance: INT32 keys (no NULLs) and one INT32 payload.

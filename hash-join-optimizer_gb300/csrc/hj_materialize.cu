@@ -24,6 +24,16 @@
 #include "hj_kernels.h"
 
 namespace hj {
+
+// One output page of a VARCHAR column (declared in hj_kernels.h).
+struct PageDesc {
+    uint64_t row;    // first row (normal page) or the string's row (long page)
+    uint32_t count;  // rows on a normal page; 0 for a long-string page
+    uint32_t nn;     // non-NULL rows (normal page)
+    uint32_t bytes;  // string bytes (normal page)
+    uint32_t chunk;  // long-string page number within the string
+};
+
 namespace {
 
 constexpr int      kMT        = 256;
@@ -101,13 +111,6 @@ __device__ __forceinline__ uint32_t loc_len(uint64_t loc, const uint8_t* base, u
     return uint32_t(f);
 }
 
-struct PageDesc {
-    uint64_t row;    // first row (normal page) or the string's row (long page)
-    uint32_t count;  // rows on a normal page; 0 for a long-string page
-    uint32_t nn;     // non-NULL rows (normal page)
-    uint32_t bytes;  // string bytes (normal page)
-    uint32_t chunk;  // long-string page number within the string
-};
 
 // Greedy packing of one tile by one warp.  With desc == nullptr only counts.
 __device__ uint32_t pack_tile(const uint64_t* ol, const uint8_t* base, uint64_t npages, uint64_t t0,
@@ -175,28 +178,53 @@ __device__ uint32_t pack_tile(const uint64_t* ol, const uint8_t* base, uint64_t 
     return npg;
 }
 
-// Gathers the tile's locators through the row ids into `ol` (read back by the
-// later passes in output order) and counts the tile's pages.
-__global__ void k_pack_count(const uint64_t* __restrict__ locs, const uint32_t* __restrict__ rid,
-                             uint64_t* __restrict__ ol, const uint8_t* __restrict__ base, uint64_t npages,
-                             uint64_t n, uint64_t ntiles, uint32_t* __restrict__ tile_pages) {
-    const uint64_t t = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-    if (t >= ntiles) return;
-    const uint64_t t0 = t * kStrTile, t1 = (n < t0 + kStrTile ? n : t0 + kStrTile);
-    for (uint64_t i = t0 + (threadIdx.x & 31); i < t1; i += 32)
-        ol[i] = __ldg(locs + (rid ? uint64_t(__ldg(rid + i)) : i));
-    __syncwarp();
-    const uint32_t c = pack_tile(ol, base, npages, t0, t1, nullptr);
-    if ((threadIdx.x & 31) == 0) tile_pages[t] = c;
+// The VARCHAR output columns of one materialisation are packed together:
+// warp w of a launch takes tile w of the concatenated tile lists, so short
+// columns share the GPU instead of each filling a fraction of it.
+constexpr int kMaxPackCols = 8;
+struct PackCol {
+    const uint64_t* locs;
+    const uint32_t* rid;
+    uint64_t*       ol;
+    const uint8_t*  base;
+    uint64_t        npages, n, ntiles, tile_base;
+    uint32_t*       tile_pages;
+    const uint64_t* tile_off;
+    PageDesc*       desc;
+};
+struct PackCols {
+    int     n;
+    PackCol c[kMaxPackCols];
+};
+
+__device__ __forceinline__ int pack_col_of(const PackCols& P, uint64_t t) {
+    int c = 0;
+    while (c + 1 < P.n && P.c[c + 1].tile_base <= t) ++c;
+    return c;
 }
 
-__global__ void k_pack_emit(const uint64_t* __restrict__ ol, const uint8_t* __restrict__ base, uint64_t npages,
-                            uint64_t n, uint64_t ntiles, const uint64_t* __restrict__ tile_off,
-                            PageDesc* __restrict__ desc) {
-    const uint64_t t = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-    if (t >= ntiles) return;
-    const uint64_t t0 = t * kStrTile, t1 = (n < t0 + kStrTile ? n : t0 + kStrTile);
-    pack_tile(ol, base, npages, t0, t1, desc + tile_off[t]);
+// Gathers the tile's locators through the row ids into `ol` (read back by the
+// later passes in output order) and counts the tile's pages.
+__global__ void k_pack_count(PackCols P, uint64_t ntiles) {
+    const uint64_t g = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    if (g >= ntiles) return;
+    const PackCol& v  = P.c[pack_col_of(P, g)];
+    const uint64_t t  = g - v.tile_base;
+    const uint64_t t0 = t * kStrTile, t1 = (v.n < t0 + kStrTile ? v.n : t0 + kStrTile);
+    for (uint64_t i = t0 + (threadIdx.x & 31); i < t1; i += 32)
+        v.ol[i] = __ldg(v.locs + (v.rid ? uint64_t(__ldg(v.rid + i)) : i));
+    __syncwarp();
+    const uint32_t c = pack_tile(v.ol, v.base, v.npages, t0, t1, nullptr);
+    if ((threadIdx.x & 31) == 0) v.tile_pages[t] = c;
+}
+
+__global__ void k_pack_emit(PackCols P, uint64_t ntiles) {
+    const uint64_t g = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    if (g >= ntiles) return;
+    const PackCol& v  = P.c[pack_col_of(P, g)];
+    const uint64_t t  = g - v.tile_base;
+    const uint64_t t0 = t * kStrTile, t1 = (v.n < t0 + kStrTile ? v.n : t0 + kStrTile);
+    pack_tile(v.ol, v.base, v.npages, t0, t1, v.desc + v.tile_off[t]);
 }
 
 // Copies `len` bytes of a normal string from global `src` (inside an input
@@ -322,32 +350,66 @@ void launch_write_int32_pages(const IntCol& col, const uint32_t* rid, uint64_t n
     HJ_LAUNCH_CHECK();
 }
 
-void varchar_plan(VarcharOut& v, cudaStream_t st) {
-    if (v.n == 0) return;
-    v.ol         = dalloc_n<uint64_t>(v.n, st);
-    v.ntiles     = (v.n + kStrTile - 1) / kStrTile;
-    v.tile_pages = dalloc_n<uint32_t>(v.ntiles, st);
-    v.tile_off   = dalloc_n<uint64_t>(v.ntiles + 1, st);
-    k_pack_count<<<div_up(v.ntiles * 32, 128), 128, 0, st>>>(v.locs, v.rid, v.ol, v.base, v.base_pages, v.n,
-                                                            v.ntiles, v.tile_pages);
-    HJ_LAUNCH_CHECK();
-    scan_exclusive_u32_to_u64(v.tile_pages, v.tile_off, v.ntiles, st);
+namespace {
+// The columns of `vs` (n > 0 rows) in groups of kMaxPackCols, as launch parameters.
+template <class F>
+void for_pack_groups(std::vector<VarcharOut*>& vs, F&& f) {
+    std::vector<VarcharOut*> live;
+    for (auto* v : vs)
+        if (v->n) live.push_back(v);
+    for (size_t g0 = 0; g0 < live.size(); g0 += kMaxPackCols) {
+        PackCols P{};
+        uint64_t tiles = 0;
+        for (size_t i = g0; i < std::min(live.size(), g0 + kMaxPackCols); ++i) {
+            VarcharOut& v = *live[i];
+            P.c[P.n++]    = PackCol{v.locs, v.rid, v.ol, v.base, v.base_pages, v.n, v.ntiles, tiles,
+                                 v.tile_pages, v.tile_off, v.desc};
+            tiles += v.ntiles;
+        }
+        f(P, tiles);
+    }
+}
+}  // namespace
+
+void varchar_plan(std::vector<VarcharOut*>& vs, cudaStream_t st) {
+    for (auto* vp : vs) {
+        VarcharOut& v = *vp;
+        if (v.n == 0) continue;
+        v.ol         = dalloc_n<uint64_t>(v.n, st);
+        v.ntiles     = (v.n + kStrTile - 1) / kStrTile;
+        v.tile_pages = dalloc_n<uint32_t>(v.ntiles, st);
+        v.tile_off   = dalloc_n<uint64_t>(v.ntiles + 1, st);
+    }
+    for_pack_groups(vs, [&](const PackCols& P, uint64_t tiles) {
+        k_pack_count<<<div_up(tiles * 32, 128), 128, 0, st>>>(P, tiles);
+        HJ_LAUNCH_CHECK();
+    });
+    for (auto* vp : vs)
+        if (vp->n) scan_exclusive_u32_to_u64(vp->tile_pages, vp->tile_off, vp->ntiles, st);
 }
 
-uint8_t* varchar_write(VarcharOut& v, uint64_t pages, cudaStream_t st) {
-    if (v.n == 0) return nullptr;
-    auto* desc = static_cast<PageDesc*>(dalloc(std::max<uint64_t>(pages, 1) * sizeof(PageDesc), st));
-    k_pack_emit<<<div_up(v.ntiles * 32, 128), 128, 0, st>>>(v.ol, v.base, v.base_pages, v.n, v.ntiles, v.tile_off,
-                                                           desc);
-    HJ_LAUNCH_CHECK();
-    auto* out = static_cast<uint8_t*>(dalloc(std::max<uint64_t>(pages, 1) * kPage, st));
-
-    k_write_varchar_pages<<<grid_of(pages), kMT, 0, st>>>(desc, pages, v.ol, v.base, v.base_pages, out);
-    HJ_LAUNCH_CHECK();
-    for (void* p : {(void*)desc, (void*)v.ol, (void*)v.tile_pages, (void*)v.tile_off}) dfree(p, st);
-    v.ol         = nullptr;
-    v.tile_pages = nullptr;
-    v.tile_off   = nullptr;
+std::vector<uint8_t*> varchar_write(std::vector<VarcharOut*>& vs, const std::vector<uint64_t>& pages,
+                                    cudaStream_t st) {
+    std::vector<uint8_t*> out(vs.size(), nullptr);
+    for (size_t i = 0; i < vs.size(); ++i)
+        if (vs[i]->n) vs[i]->desc = static_cast<PageDesc*>(dalloc(std::max<uint64_t>(pages[i], 1) * sizeof(PageDesc), st));
+    for_pack_groups(vs, [&](const PackCols& P, uint64_t tiles) {
+        k_pack_emit<<<div_up(tiles * 32, 128), 128, 0, st>>>(P, tiles);
+        HJ_LAUNCH_CHECK();
+    });
+    for (size_t i = 0; i < vs.size(); ++i) {
+        VarcharOut& v = *vs[i];
+        if (v.n == 0) continue;
+        out[i] = static_cast<uint8_t*>(dalloc(std::max<uint64_t>(pages[i], 1) * kPage, st));
+        k_write_varchar_pages<<<grid_of(pages[i]), kMT, 0, st>>>(v.desc, pages[i], v.ol, v.base, v.base_pages,
+                                                                 out[i]);
+        HJ_LAUNCH_CHECK();
+        for (void* p : {(void*)v.desc, (void*)v.ol, (void*)v.tile_pages, (void*)v.tile_off}) dfree(p, st);
+        v.desc       = nullptr;
+        v.ol         = nullptr;
+        v.tile_pages = nullptr;
+        v.tile_off   = nullptr;
+    }
     return out;
 }
 
