@@ -37,6 +37,7 @@ EXPORTS = [
     "hj_pages_from_int32", "hj_pages_from_strings", "hj_table_probe_noalloc",
     "hj_batch_execute", "hj_batch_generate", "hj_table_prepare",
     "hj_server_create", "hj_server_submit", "hj_server_wait", "hj_server_info", "hj_server_destroy",
+    "hj_table_dump", "hj_table_load",
 ]
 BATCH_PERSISTENT, BATCH_PLAIN = 0, 1
 NOALLOC_MAX_PROBE_ROWS = 65536  # HJ_NOALLOC_MAX_PROBE_ROWS
@@ -141,6 +142,8 @@ def lib() -> C.CDLL:
     L.hj_batch_execute.argtypes = [vp, P(BatchInstance), u32, i32, P(u64), P(u64), P(u32)]
     L.hj_batch_generate.argtypes = [vp, u64, u32, u32, u64, u32, u64, vp, vp]
     L.hj_table_prepare.argtypes = [vp, u64]
+    L.hj_table_dump.argtypes = [P(TableDesc), C.c_char_p]
+    L.hj_table_load.argtypes = [vp, C.c_char_p, P(u64)]
     L.hj_server_create.restype = vp
     L.hj_server_create.argtypes = [vp, P(ServerOptions)]
     L.hj_server_submit.argtypes = [vp, P(PlanDesc), P(u64)]
@@ -372,6 +375,16 @@ class Engine:
     def release(self, table: Table) -> None:
         _check(self._ctx, lib().hj_table_release(self._ctx, table.resident))
 
+    def load_table(self, path) -> Table:
+        """A table file (the reference's cache format) uploaded as a resident table."""
+        h = C.c_uint64()
+        _check(self._ctx, lib().hj_table_load(self._ctx, str(path).encode(), C.byref(h)))
+        head = np.fromfile(str(path), dtype=np.uint8, count=208)
+        num_rows, ncols = (int(x) for x in head[:16].view(np.uint64))
+        types = head[16:80].view(np.int32)[:ncols]
+        return Table(num_rows, [Column(int(t), np.zeros((0, PAGE_SIZE), np.uint8)) for t in types],
+                     resident=h.value)
+
     def prepare(self, table: Table) -> None:
         """Decodes a resident table's columns once and keeps them decoded in HBM."""
         _check(self._ctx, lib().hj_table_prepare(self._ctx, table.resident))
@@ -495,6 +508,18 @@ class Server:
 
     def __exit__(self, *exc):
         self.close()
+
+
+def dump_table(table: Table, path) -> None:
+    """Writes a host table in the reference's binary cache format (DumpTable)."""
+    cols = (ColumnDesc * max(1, len(table.columns)))()
+    keep = []
+    for j, col in enumerate(table.columns):
+        cols[j].type, cols[j].num_pages, cols[j].pages = col.type, col.num_pages, _page_ptrs(col, keep)
+    td = TableDesc(table.num_rows, len(table.columns), cols, 0)
+    rc = lib().hj_table_dump(C.byref(td), str(path).encode())
+    if rc != HJ_OK:
+        raise HjError(rc, f"hj_table_dump({path}) failed")
 
 
 # ------------------------------------------------------------ page decoding --

@@ -21,7 +21,7 @@ LIB = HERE / "libhjgb300.so"
 CUDA_SOURCES = ["hj_scan.cu", "hj_decode.cu", "hj_build.cu", "hj_probe.cu",
                 "hj_materialize.cu", "hj_transfer.cu", "hj_engine.cu", "hj_noalloc.cu",
                 "hj_batch.cu", "hj_serve.cu", "hj_filter.cu"]
-CXX_SOURCES = ["hj_pages_host.cpp", "contest.cpp"]
+CXX_SOURCES = ["hj_pages_host.cpp", "contest.cpp", "hj_cache.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

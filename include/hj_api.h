@@ -168,6 +168,13 @@ int hj_get_option(const hj_context* ctx, const char* name, int64_t* value);
  * hj_table_desc.resident.  hj_table_release frees it. */
 int hj_table_upload(hj_context* ctx, const hj_table_desc* table, uint64_t* handle);
 int hj_table_release(hj_context* ctx, uint64_t handle);
+/* Binary table files in the reference's cache format (DumpTable,
+ * include/table.h:128-211; Table::from_cache, src/build_table.cpp:147-203):
+ * hj_table_dump writes a host table (at most 16 columns); hj_table_load maps a
+ * file and uploads it as a resident table (handle as from hj_table_upload).
+ * Files written by either side load on the other. */
+int hj_table_dump(const hj_table_desc* table, const char* path);
+int hj_table_load(hj_context* ctx, const char* path, uint64_t* handle);
 /* Decodes every column of a resident table once and keeps the decoded form in
  * HBM, so later plans skip the per-call decode (no counterpart in the
  * reference: its tables are host-resident and decoded per execute). */

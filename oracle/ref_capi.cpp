@@ -10,6 +10,7 @@
 // pinned against the real thing.
 #include <cstring>
 #include <exception>
+#include <fstream>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -106,6 +107,31 @@ int ref_execute(const hj_plan_desc* desc, oracle_result* out) {
         return fail(out, HJ_ERR_RUNTIME, e.what());
     } catch (const std::exception& e) {
         return fail(out, HJ_ERR_INVALID, e.what());
+    }
+}
+
+// The reference's binary table cache: DumpTable::dump (include/table.h:128-211)
+// of a borrowed table into `path`, and Table::from_cache (src/build_table.cpp:
+// 147-203) of a file into `out`.
+int ref_dump_table(const hj_table_desc* t, const char* path) {
+    try {
+        ColumnarTable ct = borrow_table(*t);
+        DumpTable     d(&ct);
+        std::ofstream f(path, std::ios::binary);
+        d.dump(f);
+        return f.good() ? HJ_OK : HJ_ERR_RUNTIME;
+    } catch (const std::exception&) {
+        return HJ_ERR_RUNTIME;
+    }
+}
+
+int ref_from_cache(const char* path, oracle_result* out) {
+    std::memset(out, 0, sizeof(*out));
+    try {
+        fill_result(Table::from_cache(path), out);
+        return HJ_OK;
+    } catch (const std::exception& e) {
+        return fail(out, HJ_ERR_RUNTIME, e.what());
     }
 }
 
