@@ -33,20 +33,40 @@ __global__ void k_page_rows(const uint8_t* __restrict__ pages, uint64_t num_page
     rows[p] = r;
 }
 
-// One warp per page (grid-stride over pages): 32 rows at a time, each
-// non-NULL row's rank among the page's non-NULL rows comes from a ballot of
-// the bitmap bits, so no block-wide barrier is needed.
-template <class Emit>
-__device__ __forceinline__ void warp_rows(const uint8_t* pg, uint32_t nr, Emit&& emit) {
+// One warp per page (grid-stride over pages), 4 x 32 rows at a time: each
+// non-NULL row's rank among the page's non-NULL rows comes from ballots of the
+// bitmap bits, so no block-wide barrier is needed.  The bitmap bytes of the 4
+// steps are loaded together, then the 4 values (fetch), then stored, so each
+// lane has 4 independent loads in flight instead of one dependent chain.
+template <class Fetch, class Store>
+__device__ __forceinline__ void warp_rows(const uint8_t* pg, uint32_t nr, Fetch&& fetch, Store&& store) {
+    constexpr int  kU        = 4;
     const unsigned lane      = threadIdx.x & 31;
+    const unsigned lt        = (1u << lane) - 1;
     const uint8_t* bm        = pg + kPage - (nr + 7) / 8;
     uint32_t       rank_base = 0;
-    for (uint32_t c = 0; c < nr; c += 32) {
-        const uint32_t i   = c + lane;
-        const bool     on  = i < nr && ((bm[i >> 3] >> (i & 7)) & 1u);
-        const unsigned bal = __ballot_sync(0xffffffffu, on);
-        if (i < nr) emit(i, on, rank_base + __popc(bal & ((1u << lane) - 1)));
-        rank_base += __popc(bal);
+    for (uint32_t c = 0; c < nr; c += 32 * kU) {
+        bool on[kU];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            const uint32_t i = c + 32 * u + lane;
+            on[u]            = i < nr && ((bm[i >> 3] >> (i & 7)) & 1u);
+        }
+        uint32_t rank[kU];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            const unsigned bal = __ballot_sync(0xffffffffu, on[u]);
+            rank[u]            = rank_base + __popc(bal & lt);
+            rank_base += __popc(bal);
+        }
+        uint64_t v[kU];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) v[u] = fetch(on[u], rank[u]);
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            const uint32_t i = c + 32 * u + lane;
+            if (i < nr) store(i, v[u]);
+        }
     }
 }
 
@@ -63,11 +83,14 @@ __global__ void __launch_bounds__(kDecThreads)
         const uint32_t nr   = *reinterpret_cast<const uint16_t*>(pg);
         const int32_t* data = reinterpret_cast<const int32_t*>(pg + 4);
         uint64_t*      o    = out + row_start[p];
-        warp_rows(pg, nr, [&](uint32_t i, bool on, uint32_t rank) {
-            // a well-formed page has rank < num_non_null <= 2047; never read past it
-            o[i] = (on && rank < (kPage - 4) / 4) ? (uint64_t(uint32_t(__ldg(data + rank))) | value_t::TAG_INT32)
-                                                  : 0ull;
-        });
+        warp_rows(
+            pg, nr,
+            [&](bool on, uint32_t rank) {
+                // a well-formed page has rank < num_non_null <= 2047; never read past it
+                return (on && rank < (kPage - 4) / 4) ? (uint64_t(uint32_t(__ldg(data + rank))) | value_t::TAG_INT32)
+                                                      : 0ull;
+            },
+            [&](uint32_t i, uint64_t v) { o[i] = v; });
     }
 }
 
@@ -98,14 +121,17 @@ __global__ void __launch_bounds__(kDecThreads)
         const uint16_t* offs  = reinterpret_cast<const uint16_t*>(pg + 4);
         const uint64_t  data0 = p * kPage + 4 + 2 * uint64_t(nn);
         uint64_t*       o     = out + row_start[p];
-        warp_rows(pg, nr, [&](uint32_t i, bool on, uint32_t rank) {
-            uint64_t v = 0;
-            if (on && rank < nn && rank < (kPage - 4) / 2) {
-                const uint32_t start = rank == 0 ? 0u : offs[rank - 1];
-                v                    = make_loc(data0 + start, uint32_t(offs[rank]) - start, false);
-            }
-            o[i] = v;
-        });
+        warp_rows(
+            pg, nr,
+            [&](bool on, uint32_t rank) {
+                uint64_t v = 0;
+                if (on && rank < nn && rank < (kPage - 4) / 2) {
+                    const uint32_t start = rank == 0 ? 0u : offs[rank - 1];
+                    v                    = make_loc(data0 + start, uint32_t(offs[rank]) - start, false);
+                }
+                return v;
+            },
+            [&](uint32_t i, uint64_t v) { o[i] = v; });
     }
 }
 

@@ -35,7 +35,7 @@ namespace {
 constexpr int      kPT      = 256;
 constexpr int      kPI      = 8;
 constexpr int      kPTile   = kPT * kPI;
-constexpr uint32_t kSplit   = 16384;  // tuples per big-hit work unit
+constexpr uint32_t kSplit   = 2048;   // tuples per big-hit work unit (one warp each)
 
 struct ProbeTab {
     const uint64_t* dir;
@@ -291,8 +291,13 @@ __global__ void __launch_bounds__(256)
     k_write_big(ProbeTab T, Lists Ls, uint64_t n_big, const uint64_t* __restrict__ unit_off,
                 const uint32_t* __restrict__ unit_hit, const uint64_t* __restrict__ big_off, uint64_t base_pos,
                 Outs outs) {
+    // one warp per unit: most big hits are a few hundred tuples, so a whole
+    // block per unit would leave most of its lanes idle
     const uint64_t nunits = unit_off[n_big];
-    for (uint64_t u = blockIdx.x; u < nunits; u += gridDim.x) {
+    const unsigned lane   = threadIdx.x & 31;
+    const uint64_t gw     = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nw     = (uint64_t(gridDim.x) * blockDim.x) >> 5;
+    for (uint64_t u = gw; u < nunits; u += nw) {
         uint64_t h;
         if (unit_hit) {
             h = unit_hit[u];
@@ -310,8 +315,7 @@ __global__ void __launch_bounds__(256)
         const uint32_t e0   = min(Ls.b_e[h], s0 + kSplit);
         const uint32_t prow = Ls.b_row[h];
         const uint64_t pos0 = base_pos + big_off[h] + sub * kSplit;
-        for (uint32_t k = s0 + threadIdx.x; k < e0; k += blockDim.x)
-            emit(outs, pos0 + (k - s0), prow, __ldg(T.rows + k));
+        for (uint32_t k = s0 + lane; k < e0; k += 32) emit(outs, pos0 + (k - s0), prow, __ldg(T.rows + k));
     }
 }
 
