@@ -231,8 +231,9 @@ __global__ void k_pack_emit(PackCols P, uint64_t ntiles) {
 // page) to shared memory at img + dst.  Strings of up to 64 bytes: all covering
 // source words are loaded first (up to 18 independent loads in flight), then
 // aligned destination words are formed with funnel shifts and stored as 32-bit
-// words; the two boundary words, which neighbouring strings share, are stored
-// byte by byte.  Only words that overlap the string are read.
+// words; the two boundary words, which neighbouring strings share, are merged
+// into the zeroed image with a masked shared-memory OR (one instruction instead
+// of up to four byte stores).  Only words that overlap the string are read.
 __device__ __forceinline__ void copy_string(uint8_t* img, uint32_t dst, const uint8_t* src, uint32_t len) {
     if (len == 0) return;
     const uintptr_t a  = reinterpret_cast<uintptr_t>(src);
@@ -244,26 +245,38 @@ __device__ __forceinline__ void copy_string(uint8_t* img, uint32_t dst, const ui
     // start one word early when the source is less offset than the destination,
     // so that destination word j always takes source words j and j + 1
     const uint32_t  pre = sa < da ? 4u : 0u;
-    const uint32_t* ws  = reinterpret_cast<const uint32_t*>((a & ~uintptr_t(3)) - pre);
-    const uint32_t  so  = sa + pre;          // string start within the loaded words
-    const uint32_t  sh  = 8 * (so - da);     // 0, 8, 16 or 24
-    const uint32_t  nsw = (so + len + 3) / 4;  // loaded words that overlap the string
-    uint32_t        W[19];
+    const uintptr_t w0  = (a & ~uintptr_t(3)) - pre;  // source word W[0]
+    const uint32_t  so  = sa + pre;                   // string start within the words
+    const uint32_t  sh  = 8 * (so - da);              // 0, 8, 16 or 24
+    const uint32_t  nsw = (so + len + 3) / 4;         // words W[k] that overlap the string
+    // The words are read as 8-byte pairs from the 8-byte boundary at or below
+    // W[0]: W[k] = P[k + odd].  Bytes outside the string that come along are
+    // masked off below; the reads stay inside the string's input page (its
+    // data starts at byte >= 6 and ends before the bitmap) or the buffer slack.
+    const uintptr_t q0    = w0 & ~uintptr_t(7);
+    const uint32_t  odd   = uint32_t((w0 - q0) >> 2);
+    const uint32_t  first = so / 4;  // first W[k] that overlaps the string
+    const uint2*    qs    = reinterpret_cast<const uint2*>(q0);
+    uint32_t        P[20];
 #pragma unroll
-    for (int k = 0; k < 19; ++k) W[k] = (uint32_t(k) < nsw && (4u * k + 3 >= so)) ? __ldg(ws + k) : 0u;
+    for (int q = 0; q < 10; ++q) {
+        const bool  need = uint32_t(2 * q) < odd + nsw && uint32_t(2 * q + 1) >= odd + first;
+        const uint2 v    = need ? __ldg(qs + q) : make_uint2(0u, 0u);
+        P[2 * q]         = v.x;
+        P[2 * q + 1]     = v.y;
+    }
     const uint32_t ndw = (da + len + 3) / 4;  // destination words touched
     uint32_t*      wd  = reinterpret_cast<uint32_t*>(img + (dst & ~3u));
 #pragma unroll
     for (int j = 0; j < 18; ++j) {
         if (uint32_t(j) >= ndw) break;
-        const uint32_t D = __funnelshift_r(W[j], W[j + 1], sh);
+        const uint32_t D = __funnelshift_r(odd ? P[j + 1] : P[j], odd ? P[j + 2] : P[j + 1], sh);
         if (j == 0 || uint32_t(j) == ndw - 1) {
-            // boundary word: only the bytes of this string
-#pragma unroll
-            for (int b = 0; b < 4; ++b) {
-                const int pos = 4 * j + b - int(da);
-                if (pos >= 0 && pos < int(len)) img[(dst & ~3u) + 4 * j + b] = uint8_t(D >> (8 * b));
-            }
+            // boundary word: only the bytes of this string, bytes [lo, hi) of the word
+            const int      lo   = j == 0 ? int(da) : 0;
+            const int      hi   = min(4, int(da) + int(len) - 4 * j);
+            const uint32_t mask = (hi >= 4 ? 0xffffffffu : ((1u << (8 * hi)) - 1u)) & ~((1u << (8 * lo)) - 1u);
+            atomicOr(wd + j, D & mask);
         } else {
             wd[j] = D;
         }
