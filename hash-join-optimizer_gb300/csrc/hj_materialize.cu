@@ -127,10 +127,13 @@ __device__ uint32_t pack_tile(const uint64_t* ol, const uint8_t* base, uint64_t 
         n = m = D = 0;
         pstart    = row_end;
     };
+    // the next batch's locators are loaded while the current one is packed
+    uint64_t next = t0 + lane < t1 ? ol[t0 + lane] : 0;
     for (uint64_t b0 = t0; b0 < t1; b0 += 32) {
         const uint64_t r      = b0 + lane;
         const bool     in     = r < t1;
-        const uint64_t loc    = in ? ol[r] : 0;
+        const uint64_t loc    = next;
+        next                  = b0 + 32 + lane < t1 ? ol[b0 + 32 + lane] : 0;
         const bool     nn     = loc != 0;
         const uint32_t len    = nn ? loc_len(loc, base, npages) : 0;
         const bool     lng    = nn && len > kLongLimit;
