@@ -43,17 +43,26 @@ std::atomic<uint64_t> g_kernel_launches{0};
 // ---------------------------------------------------------------- memory ----
 
 // Large blocks (result pages, decoded columns, row-id streams: >= 64 MB) are
-// kept per stream when freed and handed back to the next allocation of a
-// similar size on the same stream, without going through the pool: stream
-// order makes the reuse safe, and the host never waits on the pool's memory
-// mapping between two kernels.  flush_stream() returns a stream's blocks.
+// kept per stream when freed on the stream that allocated them, and handed
+// back to the next allocation of a similar size on that stream without going
+// through the pool: stream order makes the reuse safe, and the host never
+// waits on the pool's memory mapping between two kernels.  A block freed on
+// another stream (a served result, freed through the server's context) goes
+// back to the pool, and a stream keeps at most kKeepPerStream bytes.
+// flush_stream() returns a stream's blocks.
 namespace {
-constexpr size_t kBig     = size_t(64) << 20;
-constexpr size_t kGranule = size_t(16) << 20;
+constexpr size_t kBig           = size_t(64) << 20;
+constexpr size_t kGranule       = size_t(16) << 20;
+constexpr size_t kKeepPerStream = size_t(48) << 30;
+struct BigBlock {
+    size_t       bytes;
+    cudaStream_t owner;  // the stream that allocated it
+};
 struct BigBlocks {
-    std::mutex                                                mu;
+    std::mutex                                                     mu;
     std::unordered_map<cudaStream_t, std::multimap<size_t, void*>> free;
-    std::unordered_map<void*, size_t>                          size;
+    std::unordered_map<cudaStream_t, size_t>                       kept;  // bytes in `free` per stream
+    std::unordered_map<void*, BigBlock>                            size;
 };
 BigBlocks& big_blocks() {
     static BigBlocks* b = new BigBlocks();  // outlives every context
@@ -80,6 +89,7 @@ void flush_stream(cudaStream_t st) {
         cudaFreeAsync(kv.second, st);
     }
     b.free.erase(it);
+    b.kept.erase(st);
 }
 
 void* dalloc(size_t bytes, cudaStream_t st) {
@@ -93,6 +103,7 @@ void* dalloc(size_t bytes, cudaStream_t st) {
             auto                        it = m.lower_bound(bytes);
             if (it != m.end() && it->first <= bytes + bytes / 4) {
                 void* p = it->second;
+                b.kept[st] -= it->first;
                 m.erase(it);
                 return p;
             }
@@ -110,7 +121,7 @@ void* dalloc(size_t bytes, cudaStream_t st) {
         }
         if (!p) throw Error(HJ_ERR_NOMEM, "device allocation of " + std::to_string(bytes) + " bytes failed");
         std::lock_guard<std::mutex> g(b.mu);
-        b.size[p] = bytes;
+        b.size[p] = BigBlock{bytes, st};
         return p;
     }
     void* p = pool_alloc(bytes, st);
@@ -125,8 +136,13 @@ void dfree(void* p, cudaStream_t st) {
         std::lock_guard<std::mutex> g(b.mu);
         auto                        it = b.size.find(p);
         if (it != b.size.end()) {
-            b.free[st].emplace(it->second, p);
-            return;
+            const size_t bytes = it->second.bytes;
+            if (it->second.owner == st && b.kept[st] + bytes <= kKeepPerStream) {
+                b.free[st].emplace(bytes, p);
+                b.kept[st] += bytes;
+                return;
+            }
+            b.size.erase(it);  // back to the pool
         }
     }
     cudaFreeAsync(p, st);
