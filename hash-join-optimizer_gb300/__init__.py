@@ -37,7 +37,7 @@ EXPORTS = [
     "hj_pages_from_int32", "hj_pages_from_strings", "hj_table_probe_noalloc",
     "hj_batch_execute", "hj_batch_generate", "hj_table_prepare",
     "hj_server_create", "hj_server_submit", "hj_server_wait", "hj_server_info", "hj_server_destroy",
-    "hj_table_dump", "hj_table_load",
+    "hj_table_dump", "hj_table_load", "hj_host_register", "hj_host_unregister",
 ]
 BATCH_PERSISTENT, BATCH_PLAIN = 0, 1
 NOALLOC_MAX_PROBE_ROWS = 65536  # HJ_NOALLOC_MAX_PROBE_ROWS
@@ -130,6 +130,8 @@ def lib() -> C.CDLL:
     L.hj_result_column.argtypes = [vp, u32, P(i32), P(u64)]
     L.hj_result_copy_pages.argtypes = [vp, vp, u32, P(vp)]
     L.hj_result_copy_contiguous.argtypes = [vp, vp, u32, vp]
+    L.hj_host_register.argtypes = [vp, u64]
+    L.hj_host_unregister.argtypes = [vp]
     L.hj_result_stats.argtypes = [vp, P(u64), P(u64), P(u64)]
     L.hj_result_free.argtypes = [vp]
     L.hj_table_build.argtypes = [vp, vp, vp, u64, i32, P(vp)]
@@ -295,6 +297,18 @@ def _page_ptrs(col: "Column", keep: list):
     arr = np.arange(max(1, col.num_pages), dtype=np.uint64) * np.uint64(PAGE_SIZE) + np.uint64(col.pages.ctypes.data)
     keep.append(arr)
     return arr.ctypes.data_as(C.POINTER(C.c_void_p))
+
+
+def host_register(a: np.ndarray) -> None:
+    """Page-locks the memory of a contiguous array (hj_host_register): input
+    pages and result buffers there move through the copy engines."""
+    if not a.flags.c_contiguous or a.nbytes == 0:
+        raise ValueError("host_register needs a non-empty contiguous array")
+    _check(None, lib().hj_host_register(a.ctypes.data, a.nbytes))
+
+
+def host_unregister(a: np.ndarray) -> None:
+    _check(None, lib().hj_host_unregister(a.ctypes.data))
 
 
 def _check(ctx, rc: int) -> None:

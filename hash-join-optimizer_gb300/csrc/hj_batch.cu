@@ -779,7 +779,7 @@ void plain_instance(const BatchInstance& b, const ProbeParams& prm, int dir_bits
         np    = total;
         if (last) rows = total;
     }
-    HJ_CUDA(cudaMemcpyAsync(prm.pinned, d_sum, 8, cudaMemcpyDeviceToHost, st));
+    readback(prm.pinned, d_sum, 8, true, st);  // page-locked scratch
     HJ_CUDA(cudaStreamSynchronize(st));
     sum = prm.pinned[0];
 }

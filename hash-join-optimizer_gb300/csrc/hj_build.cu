@@ -355,7 +355,7 @@ void build_table(const KeyCol& kc, int dir_bits, int radix_bits, Table& t, uint6
         k_part_hist<<<grid_for(kc.n, kThreads), kThreads, smem, st>>>(kc, r, part_cnt, d_nvalid);
         HJ_LAUNCH_CHECK();
         if (n_valid < 0) {
-            HJ_CUDA(cudaMemcpyAsync(scratch_host, d_nvalid, sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+            readback(scratch_host, d_nvalid, sizeof(uint64_t), true, st);  // page-locked scratch
             HJ_CUDA(cudaStreamSynchronize(st));
         }
     };

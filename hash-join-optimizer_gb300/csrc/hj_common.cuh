@@ -109,25 +109,34 @@ struct Filters {
     Filt f[kMaxFilters];
 };
 
-// Does base row r pass every filter?  NULL never compares true; IS_NULL /
+// Comparisons as truth tables over a value's state: 0 greater than the
+// literal, 1 equal, 2 less, 3 NULL.  NULL never compares true; IS_NULL /
 // IS_NOT_NULL test validity (the reference's bitmap & comparison).
+__host__ __device__ __forceinline__ uint32_t cmp_table(int32_t op) {
+    switch (op) {
+        case HJ_CMP_EQ: return 0x2u;
+        case HJ_CMP_NEQ: return 0x5u;
+        case HJ_CMP_LT: return 0x4u;
+        case HJ_CMP_GT: return 0x1u;
+        case HJ_CMP_LEQ: return 0x6u;
+        case HJ_CMP_GEQ: return 0x3u;
+        case HJ_CMP_IS_NULL: return 0x8u;
+        default: return 0x7u;  // HJ_CMP_IS_NOT_NULL
+    }
+}
+__device__ __forceinline__ uint32_t cmp_state(bool valid, int32_t v, int32_t x) {
+    return valid ? (v < x ? 2u : (v == x ? 1u : 0u)) : 3u;
+}
+__device__ __forceinline__ bool cmp_ok(int32_t op, bool valid, int32_t v, int32_t x) {
+    return (cmp_table(op) >> cmp_state(valid, v, x)) & 1u;
+}
+
+// Does base row r pass every filter?
 __device__ __forceinline__ bool filt_pass(const Filters& F, uint64_t r) {
     for (int i = 0; i < F.n; ++i) {
         int32_t    v     = 0;
         const bool valid = int_get(F.f[i].col, r, v);
-        const int32_t x  = F.f[i].val;
-        bool          ok;
-        switch (F.f[i].op) {
-            case HJ_CMP_EQ: ok = valid && v == x; break;
-            case HJ_CMP_NEQ: ok = valid && v != x; break;
-            case HJ_CMP_LT: ok = valid && v < x; break;
-            case HJ_CMP_GT: ok = valid && v > x; break;
-            case HJ_CMP_LEQ: ok = valid && v <= x; break;
-            case HJ_CMP_GEQ: ok = valid && v >= x; break;
-            case HJ_CMP_IS_NULL: ok = !valid; break;
-            default: ok = valid; break;  // HJ_CMP_IS_NOT_NULL
-        }
-        if (!ok) return false;
+        if (!cmp_ok(F.f[i].op, valid, v, F.f[i].val)) return false;
     }
     return true;
 }

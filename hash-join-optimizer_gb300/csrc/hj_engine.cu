@@ -350,6 +350,7 @@ struct hj_context {
     std::unique_ptr<hj::ThreadPool>         pool;
     std::shared_ptr<hj::Store> store;  // resident tables (shared with cloned serving slots)
     int64_t             table_cache = 0;     // reuse tables built over resident base columns
+    int64_t             fuse_filters = 0;    // evaluate a probe side's scan predicate inside the probe
 };
 
 struct hj_result {
@@ -451,43 +452,18 @@ void download_pages(hj_context* c, const uint8_t* src, uint64_t n, void* const* 
 
 bool direct_host_access(const hj_context* c) { return c->ats_capable && c->host_access; }
 
-// Uploads the listed columns of a host table (others stay empty).  With
-// direct host access the GPU gathers the pages itself and the page headers
-// come back in one copy for all columns; otherwise host threads stage them.
+// Uploads the listed columns of a host table (others stay empty).  Pages in
+// page-locked memory go through the copy engines, one copy per run of
+// consecutive pages; otherwise, with direct host access, the GPU gathers the
+// pages itself; in both cases the page headers come back in one copy for all
+// columns.  Without either, host threads stage the pages.
 std::shared_ptr<DevTable> upload_table(hj_context* c, const hj_table_desc& t,
                                        const std::vector<bool>& want) {
+    constexpr size_t kMaxRuns = 64;
     auto dt      = std::make_shared<DevTable>();
     dt->num_rows = t.num_rows;
     dt->cols.resize(t.num_columns);
-    if (direct_host_access(c)) {
-        std::vector<std::vector<uint16_t>> hnr(t.num_columns), hnn(t.num_columns);
-        std::vector<Buf>                   dhdr(t.num_columns);
-        for (uint32_t i = 0; i < t.num_columns; ++i) {
-            DevColumn& d = dt->cols[i];
-            d.type       = t.columns[i].type;
-            d.num_pages  = t.columns[i].num_pages;
-            if (!want.empty() && !want[i]) continue;
-            d.pages = make_buf(std::max<uint64_t>(d.num_pages, 1) * kPage + 256, c->st);
-            if (d.num_pages == 0) continue;
-            dhdr[i]       = make_buf(d.num_pages * 4, c->st);
-            uint16_t* dnr = dhdr[i]->as<uint16_t>();
-            launch_gather_host_pages(t.columns[i].pages, d.num_pages, d.pages->as<uint8_t>(), dnr,
-                                     dnr + d.num_pages, c->st);
-        }
-        for (uint32_t i = 0; i < t.num_columns; ++i) {
-            if (!dhdr[i]) continue;
-            const uint64_t np = dt->cols[i].num_pages;
-            hnr[i].resize(np);
-            hnn[i].resize(np);
-            HJ_CUDA(cudaMemcpyAsync(hnr[i].data(), dhdr[i]->p, np * 2, cudaMemcpyDeviceToHost, c->st));
-            HJ_CUDA(cudaMemcpyAsync(hnn[i].data(), dhdr[i]->as<uint16_t>() + np, np * 2, cudaMemcpyDeviceToHost,
-                                    c->st));
-        }
-        HJ_CUDA(cudaStreamSynchronize(c->st));
-        for (uint32_t i = 0; i < t.num_columns; ++i)
-            if (dt->cols[i].pages) page_stats(dt->cols[i], hnr[i].data(), hnn[i].data());
-        return dt;
-    }
+    std::vector<Buf> dhdr(t.num_columns);
     std::vector<uint16_t> nr, nn;
     for (uint32_t i = 0; i < t.num_columns; ++i) {
         DevColumn& d = dt->cols[i];
@@ -497,11 +473,46 @@ std::shared_ptr<DevTable> upload_table(hj_context* c, const hj_table_desc& t,
         // 256 bytes of slack: no kernel reads past the pages, but word loads near
         // the end of the last page never touch another allocation
         d.pages = make_buf(std::max<uint64_t>(d.num_pages, 1) * kPage + 256, c->st);
+        if (d.num_pages == 0) {
+            page_stats(d, nullptr, nullptr);
+            continue;
+        }
+        const std::vector<PageRun> runs = locked_runs(t.columns[i].pages, d.num_pages, kMaxRuns);
+        if (!runs.empty() || direct_host_access(c)) {
+            dhdr[i]       = make_buf(d.num_pages * 4, c->st);
+            uint16_t* dnr = dhdr[i]->as<uint16_t>();
+            if (!runs.empty()) {
+                for (const PageRun& r : runs)
+                    HJ_CUDA(cudaMemcpyAsync(d.pages->as<uint8_t>() + r.first * kPage, t.columns[i].pages[r.first],
+                                            r.count * kPage, cudaMemcpyHostToDevice, c->st));
+                launch_page_headers(d.pages->as<uint8_t>(), d.num_pages, dnr, dnr + d.num_pages, c->st);
+            } else {
+                launch_gather_host_pages(t.columns[i].pages, d.num_pages, d.pages->as<uint8_t>(), dnr,
+                                         dnr + d.num_pages, c->st);
+            }
+            continue;
+        }
         nr.assign(d.num_pages, 0);
         nn.assign(d.num_pages, 0);
         upload_pages(c, t.columns[i].pages, d.num_pages, d.pages->as<uint8_t>(), nr.data(), nn.data());
         page_stats(d, nr.data(), nn.data());
-        if (std::getenv("HJ_TRACE_UPLOAD"))
+    }
+    std::vector<std::vector<uint16_t>> hnr(t.num_columns), hnn(t.num_columns);
+    bool                               any = false;
+    for (uint32_t i = 0; i < t.num_columns; ++i) {
+        if (!dhdr[i]) continue;
+        const uint64_t np = dt->cols[i].num_pages;
+        hnr[i].resize(np);
+        hnn[i].resize(np);
+        readback(hnr[i].data(), dhdr[i]->p, np * 2, c->ats_capable, c->st);
+        readback(hnn[i].data(), dhdr[i]->as<uint16_t>() + np, np * 2, c->ats_capable, c->st);
+        any = true;
+    }
+    if (any) HJ_CUDA(cudaStreamSynchronize(c->st));
+    for (uint32_t i = 0; i < t.num_columns; ++i) {
+        if (dhdr[i]) page_stats(dt->cols[i], hnr[i].data(), hnn[i].data());
+        const DevColumn& d = dt->cols[i];
+        if (d.pages && std::getenv("HJ_TRACE_UPLOAD"))
             std::fprintf(stderr, "[hj upload] column %u type %d pages %llu rows %llu non_null %llu dense1984 %d\n", i,
                          d.type, (unsigned long long)d.num_pages, (unsigned long long)d.rows,
                          (unsigned long long)d.non_null, int(d.dense1984));
@@ -722,8 +733,10 @@ struct Exec {
             throw Error(HJ_ERR_INVALID, "join attribute out of range");
         const ColRef bk = B.cols[battr], pk = P.cols[pattr];
         // A filtered build side is compacted; a filtered probe side is read raw
-        // and its predicate evaluated by the probe's count pass.
+        // and its predicate evaluated by the probe's count pass (option
+        // "fuse_filters", else compacted too).
         compact(B);
+        if (!c->fuse_filters) compact(P);
         // Non-INT32 join keys: the reference throws on the first non-NULL value
         // (execute.cpp:81,130).
         for (auto [in, cr] : {std::pair<Inter*, ColRef>{&B, bk}, std::pair<Inter*, ColRef>{&P, pk}}) {
@@ -893,8 +906,8 @@ struct Exec {
         if (!vout.empty()) {  // one synchronisation for the page counts of every VARCHAR column
             phase("mat_sync");
             for (size_t i = 0; i < vout.size(); ++i)
-                HJ_CUDA(cudaMemcpyAsync(c->pinned + i, vout[i].second.tile_off + vout[i].second.ntiles,
-                                        sizeof(uint64_t), cudaMemcpyDeviceToHost, c->st));
+                readback(c->pinned + i, vout[i].second.tile_off + vout[i].second.ntiles, sizeof(uint64_t), true,
+                         c->st);  // page-locked scratch
             HJ_CUDA(cudaStreamSynchronize(c->st));
             vpages.assign(c->pinned, c->pinned + vout.size());
         }
@@ -978,6 +991,7 @@ hj_context* context_clone(const hj_context* p) {
     c->dir_cap_bits = p->dir_cap_bits;
     c->host_access  = p->host_access;
     c->table_cache  = p->table_cache;
+    c->fuse_filters = p->fuse_filters;
     return c;
 }
 
@@ -1076,6 +1090,8 @@ int hj_set_option(hj_context* c, const char* name, int64_t v) {
         c->host_access = v != 0;
     } else if (n == "table_cache") {
         c->table_cache = v != 0;
+    } else if (n == "fuse_filters") {
+        c->fuse_filters = v != 0;
     } else if (n == "batch_load_pct") {
         if (v < 10 || v > 800) return HJ_ERR_INVALID;
         c->batch_load_pct = v;
@@ -1103,6 +1119,7 @@ int hj_get_option(const hj_context* c, const char* name, int64_t* v) {
     else if (n == "host_access") *v = c->host_access;
     else if (n == "host_access_capable") *v = c->ats_capable;
     else if (n == "table_cache") *v = c->table_cache;
+    else if (n == "fuse_filters") *v = c->fuse_filters;
     else if (n == "batch_load_pct") *v = c->batch_load_pct;
     else if (n == "batch_graph") *v = c->batch_graph;
     else if (n == "batch_part_log2") *v = c->batch_part_log2;
@@ -1251,12 +1268,38 @@ int hj_result_column(const hj_result* r, uint32_t col, int32_t* type, uint64_t* 
     return HJ_OK;
 }
 
+int hj_host_register(void* ptr, uint64_t bytes) {
+    if (!ptr || !bytes) return HJ_ERR_INVALID;
+    const cudaError_t e = cudaHostRegister(ptr, bytes, cudaHostRegisterDefault);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        return e == cudaErrorHostMemoryAlreadyRegistered ? HJ_ERR_INVALID : HJ_ERR_CUDA;
+    }
+    return HJ_OK;
+}
+
+int hj_host_unregister(void* ptr) {
+    if (!ptr) return HJ_ERR_INVALID;
+    const cudaError_t e = cudaHostUnregister(ptr);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        return e == cudaErrorHostMemoryNotRegistered ? HJ_ERR_INVALID : HJ_ERR_CUDA;
+    }
+    return HJ_OK;
+}
+
 int hj_result_copy_pages(hj_context* c, const hj_result* r, uint32_t col, void* const* dst) {
     if (!c || !r || col >= r->cols.size()) return HJ_ERR_INVALID;
     return hj::guarded(c, [&] {
         const auto& oc = r->cols[col];
         if (!oc.num_pages) return;
-        if (hj::direct_host_access(c)) {
+        const auto runs = hj::locked_runs(dst, oc.num_pages, 64);
+        if (!runs.empty()) {  // page-locked destination: copy engines, one copy per run
+            for (const auto& q : runs)
+                HJ_CUDA(cudaMemcpyAsync(dst[q.first], oc.pages->as<uint8_t>() + q.first * hj::kPage,
+                                        q.count * hj::kPage, cudaMemcpyDeviceToHost, c->st));
+            HJ_CUDA(cudaStreamSynchronize(c->st));
+        } else if (hj::direct_host_access(c)) {
             hj::launch_scatter_host_pages(oc.pages->as<uint8_t>(), oc.num_pages, dst, nullptr, c->st);
             HJ_CUDA(cudaStreamSynchronize(c->st));
         } else {
@@ -1270,7 +1313,10 @@ int hj_result_copy_contiguous(hj_context* c, const hj_result* r, uint32_t col, v
     return hj::guarded(c, [&] {
         const auto& oc = r->cols[col];
         if (!oc.num_pages) return;
-        if (hj::direct_host_access(c)) {
+        if (hj::locked_range(dst, oc.num_pages * hj::kPage)) {  // page-locked destination: copy engine
+            HJ_CUDA(cudaMemcpyAsync(dst, oc.pages->p, oc.num_pages * hj::kPage, cudaMemcpyDeviceToHost, c->st));
+            HJ_CUDA(cudaStreamSynchronize(c->st));
+        } else if (hj::direct_host_access(c)) {
             hj::launch_scatter_host_pages(oc.pages->as<uint8_t>(), oc.num_pages, nullptr, dst, c->st);
             HJ_CUDA(cudaStreamSynchronize(c->st));
         } else {

@@ -32,6 +32,23 @@ void launch_gather_host_pages(const void* const* host_pages, uint64_t n, uint8_t
 // scatter: contiguous HBM pages -> host_pages[i] (or host_contig when host_pages is null).
 void launch_scatter_host_pages(const uint8_t* src, uint64_t n, void* const* host_pages, void* host_contig,
                                cudaStream_t st);
+// Runs of consecutive host pages (page i + 1 at page i + 8192 bytes), when
+// every run lies in page-locked memory and there are at most max_runs of
+// them; otherwise empty.  Such pages move with one cudaMemcpyAsync per run.
+struct PageRun {
+    uint64_t first, count;
+};
+std::vector<PageRun> locked_runs(const void* const* pages, uint64_t n, size_t max_runs);
+// Whether [p, p + bytes) starts and ends in page-locked host memory.
+bool locked_range(const void* p, uint64_t bytes);
+// Device -> host copy of a few bytes (counters, page headers).  kernel: the
+// GPU writes `host` itself (page-locked memory, or any host memory with
+// pageable host memory access), so the readback never waits behind large
+// transfers queued on the copy engines by other streams; otherwise a
+// cudaMemcpyAsync.  Stream-ordered; the caller synchronises.
+void readback(void* host, const void* dev, uint64_t bytes, bool kernel, cudaStream_t st);
+// nr / nn (device arrays) from the headers of n device pages.
+void launch_page_headers(const uint8_t* pages, uint64_t n, uint16_t* nr, uint16_t* nn, cudaStream_t st);
 
 // ---- scans (hj_scan.cu) ---------------------------------------------------
 // out[i] = sum(in[0..i)), out[n] = total.  out has n + 1 slots.

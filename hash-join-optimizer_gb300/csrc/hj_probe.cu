@@ -411,7 +411,7 @@ uint64_t probe_count(const Table& t, const KeyCol& pk, const ProbeParams& prm, P
     HJ_LAUNCH_CHECK();
     if (prm.after_count) prm.after_count();
     pp->host = prm.pinned;
-    HJ_CUDA(cudaMemcpyAsync(pp->host, L.ctr, 6 * sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+    readback(pp->host, L.ctr, 6 * sizeof(uint64_t), true, st);  // page-locked scratch
     HJ_CUDA(cudaStreamSynchronize(st));
     pp->n_light   = pp->host[0];
     pp->n_big     = pp->host[1];
@@ -537,7 +537,7 @@ int probe_into_scratch(const Table& t, const KeyCol& pk, const ProbeParams& prm,
     k_mixed_count<<<kSMs * 2, 512, 0, st>>>(T, L);
     HJ_LAUNCH_CHECK();
     uint64_t* h = prm.pinned;
-    HJ_CUDA(cudaMemcpyAsync(h, L.ctr, 6 * sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+    readback(h, L.ctr, 6 * sizeof(uint64_t), true, st);  // page-locked scratch
     HJ_CUDA(cudaStreamSynchronize(st));
     const uint64_t n_light = h[0], n_big = h[1], n_mixed = h[2];
     const uint64_t tot_light = h[3], tot_big = h[4], total = h[3] + h[4] + h[5];

@@ -112,9 +112,9 @@ typedef struct hj_node_desc {
     uint32_t         num_attrs;
     const hj_attr*   attrs;
     /* scan nodes only: rows of the base table that pass all filters (none = all
-     * rows).  A filtered scan on the probe side of a join is evaluated inside
-     * the probe's first pass over the raw rows; elsewhere its passing rows are
-     * compacted in order. */
+     * rows).  The passing rows are compacted in order before the scan's first
+     * use; with option "fuse_filters" = 1 a filtered probe side is instead read
+     * raw and its predicate evaluated inside the probe's first pass. */
     uint32_t         num_filters;
     const hj_filter* filters;
 } hj_node_desc;
@@ -157,7 +157,10 @@ void* hj_context_stream(hj_context* ctx);
  * result pages itself; 0: host threads stage them through pinned memory),
  * "table_cache" (1: a join whose build side is a whole resident base column
  * keeps the table built over it in HBM for later plans; 0, default: every
- * execute builds its own).
+ * execute builds its own), "fuse_filters" (1: a filtered scan on the probe
+ * side of a join is evaluated inside the probe instead of compacted first;
+ * 0, default: compaction, which reads only the predicate columns of the
+ * rejected rows and measured faster at 10% selectivity).
  * hj_get_option("host_access_capable") reports whether the device can. */
 int hj_set_option(hj_context* ctx, const char* name, int64_t value);
 int hj_get_option(const hj_context* ctx, const char* name, int64_t* value);
@@ -194,6 +197,14 @@ int hj_result_copy_pages(hj_context* ctx, const hj_result* res, uint32_t col,
                          void* const* dst_pages);
 /* Same, into one contiguous host buffer of num_pages * 8192 bytes. */
 int hj_result_copy_contiguous(hj_context* ctx, const hj_result* res, uint32_t col, void* dst);
+/* Page-locks (pins) a host range for transfers, or releases it
+ * (cudaHostRegister / cudaHostUnregister, for callers without CUDA bindings).
+ * Input pages and result buffers in page-locked memory move through the copy
+ * engines, one copy per run of consecutive pages, without occupying SMs, and
+ * uploads of one plan overlap result downloads of another in the other
+ * direction of the link; pageable memory takes the GPU-gather or staged path. */
+int hj_host_register(void* ptr, uint64_t bytes);
+int hj_host_unregister(void* ptr);
 /* Kernel-side statistics of the last hj_execute on this result: number of
  * build tuples, probe tuples and output rows summed over all joins. */
 int  hj_result_stats(const hj_result* res, uint64_t* build_tuples, uint64_t* probe_tuples,
