@@ -206,28 +206,182 @@ __device__ __forceinline__ int pack_col_of(const PackCols& P, uint64_t t) {
     return c;
 }
 
-// Gathers the tile's locators through the row ids into `ol` (read back by the
-// later passes in output order) and counts the tile's pages.
-__global__ void k_pack_count(PackCols P, uint64_t ntiles) {
-    const uint64_t g = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-    if (g >= ntiles) return;
-    const PackCol& v  = P.c[pack_col_of(P, g)];
-    const uint64_t t  = g - v.tile_base;
-    const uint64_t t0 = t * kStrTile, t1 = (v.n < t0 + kStrTile ? v.n : t0 + kStrTile);
-    for (uint64_t i = t0 + (threadIdx.x & 31); i < t1; i += 32)
-        v.ol[i] = __ldg(v.locs + (v.rid ? uint64_t(__ldg(v.rid + i)) : i));
-    __syncwarp();
-    const uint32_t c = pack_tile(v.ol, v.base, v.npages, t0, t1, nullptr);
-    if ((threadIdx.x & 31) == 0) v.tile_pages[t] = c;
+// Packing by prefix sums.  A row costs 8 * (2 + length) + 1 eighths of a
+// byte when non-NULL (offset, string bytes, bitmap bit) and 1 when NULL; a
+// page of rows [a, b) fits when 32 + sum(cost) + 7 <= 65536 eighths (header,
+// bitmap rounded up to whole bytes), i.e. sum(cost) <= kCap.  With S_i the
+// tile's exclusive prefix of costs and T = kCap - (largest cost in the tile),
+// row i goes to page floor(S_i / T): a page then holds less than T + max cost
+// <= kCap, and no page is empty because no row costs more than T.  Tiles with
+// a long string or a row costing more than kCap / 8 (strings over ~1 KB) are
+// packed by the greedy rule instead (pack_tile, one warp).
+constexpr uint32_t kCap     = 65536 - 32 - 7;
+constexpr int      kPackT   = 512;                 // threads per tile block
+constexpr int      kPackRow = kStrTile / kPackT;   // consecutive rows per thread
+static_assert(kPackRow * kPackT == kStrTile, "tile split");
+
+struct TileCosts {
+    uint32_t cost[kPackRow];
+    uint32_t nn, len;  // this thread's non-NULL rows and string bytes
+    uint32_t maxc;
+    bool     greedy;   // a long string or a costly row in this thread's rows
+};
+
+__device__ __forceinline__ TileCosts row_costs(const uint64_t (&loc)[kPackRow], uint32_t rows) {
+    TileCosts c{};
+#pragma unroll
+    for (int k = 0; k < kPackRow; ++k) {
+        const bool     on  = uint32_t(k) < rows && loc[k] != 0;
+        const bool     lng = on && (loc[k] & kLocLong);
+        const uint32_t len = on ? uint32_t(loc_len_field(loc[k])) : 0u;
+        c.cost[k]          = uint32_t(k) >= rows ? 0u : (on ? 8u * (2u + min(len, kPage)) + 1u : 1u);
+        c.nn += on;
+        c.len += len;
+        c.maxc = max(c.maxc, c.cost[k]);
+        c.greedy |= lng || c.cost[k] > kCap / 8;
+    }
+    return c;
 }
 
-__global__ void k_pack_emit(PackCols P, uint64_t ntiles) {
-    const uint64_t g = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-    if (g >= ntiles) return;
-    const PackCol& v  = P.c[pack_col_of(P, g)];
-    const uint64_t t  = g - v.tile_base;
-    const uint64_t t0 = t * kStrTile, t1 = (v.n < t0 + kStrTile ? v.n : t0 + kStrTile);
-    pack_tile(v.ol, v.base, v.npages, t0, t1, v.desc + v.tile_off[t]);
+// Block reduction of (max, any) over the tile; every thread gets the result.
+__device__ __forceinline__ void tile_max_any(uint32_t& maxc, bool& any, uint32_t* sm) {
+    uint32_t m = maxc, a = any;
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+        m = max(m, __shfl_xor_sync(0xffffffffu, m, d));
+        a |= __shfl_xor_sync(0xffffffffu, a, d);
+    }
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+        sm[warp]      = m;
+        sm[16 + warp] = a;
+    }
+    __syncthreads();
+    m = 0;
+    a = 0;
+    for (int w = 0; w < kPackT / 32; ++w) {
+        m = max(m, sm[w]);
+        a |= sm[16 + w];
+    }
+    maxc = m;
+    any  = a != 0;
+    __syncthreads();
+}
+
+// Gathers the tile's locators through the row ids into `ol` (read back by the
+// later passes in output order) and counts the tile's pages.
+__global__ void __launch_bounds__(kPackT) k_pack_count(PackCols P, uint64_t ntiles) {
+    __shared__ uint32_t sm[33];
+    __shared__ uint64_t s_sum[kPackT / 32];
+    __shared__ uint32_t s_last;
+    for (uint64_t g = blockIdx.x; g < ntiles; g += gridDim.x) {
+        const PackCol& v  = P.c[pack_col_of(P, g)];
+        const uint64_t t  = g - v.tile_base;
+        const uint64_t t0 = t * kStrTile, t1 = (v.n < t0 + kStrTile ? v.n : t0 + kStrTile);
+        const uint64_t r0 = t0 + uint64_t(threadIdx.x) * kPackRow;
+        const uint32_t rows = r0 >= t1 ? 0u : (t1 - r0 < kPackRow ? uint32_t(t1 - r0) : uint32_t(kPackRow));
+        uint64_t       loc[kPackRow];
+#pragma unroll
+        for (int k = 0; k < kPackRow; ++k) {
+            loc[k] = 0;
+            if (uint32_t(k) < rows) {
+                const uint64_t i = r0 + k;
+                loc[k]           = __ldg(v.locs + (v.rid ? uint64_t(__ldg(v.rid + i)) : i));
+                v.ol[i]          = loc[k];
+            }
+        }
+        TileCosts c = row_costs(loc, rows);
+        // cost of the tile without its last row: the start of the last row
+        uint64_t sum = 0;
+#pragma unroll
+        for (int k = 0; k < kPackRow; ++k) {
+            sum += c.cost[k];
+            if (uint32_t(k) + 1 == rows && r0 + rows == t1) s_last = c.cost[k];
+        }
+        sum = warp_sum<uint64_t>(sum);
+        if ((threadIdx.x & 31) == 0) s_sum[threadIdx.x >> 5] = sum;
+        tile_max_any(c.maxc, c.greedy, sm);  // (its barriers also publish s_sum / s_last / ol)
+        if (c.greedy) {
+            if (threadIdx.x < 32) {
+                const uint32_t np = pack_tile(v.ol, v.base, v.npages, t0, t1, nullptr);
+                if (threadIdx.x == 0) v.tile_pages[t] = np;
+            }
+        } else if (threadIdx.x == 0) {
+            uint64_t tot = 0;
+            for (int w = 0; w < kPackT / 32; ++w) tot += s_sum[w];
+            v.tile_pages[t] = uint32_t((tot - s_last) / (kCap - c.maxc)) + 1u;
+        }
+        __syncthreads();
+    }
+}
+
+// Cost of one row from its locator (as row_costs).
+__device__ __forceinline__ uint32_t loc_cost(uint64_t loc) {
+    return loc != 0 ? 8u * (2u + min(uint32_t(loc_len_field(loc)), kPage)) + 1u : 1u;
+}
+
+// Page descriptors of each tile, at tile_off[t].
+__global__ void __launch_bounds__(kPackT) k_pack_emit(PackCols P, uint64_t ntiles) {
+    constexpr int kMaxTilePages = kStrTile / 7 + 1;  // rows cost at most kCap / 8: >= 7 rows a page
+    __shared__ uint32_t sm[33];
+    __shared__ uint64_t s_scan[33];
+    __shared__ uint16_t p_row[kMaxTilePages], p_nn[kMaxTilePages];
+    __shared__ uint32_t p_len[kMaxTilePages];
+    __shared__ uint32_t s_np;
+    for (uint64_t g = blockIdx.x; g < ntiles; g += gridDim.x) {
+        const PackCol& v  = P.c[pack_col_of(P, g)];
+        const uint64_t t  = g - v.tile_base;
+        const uint64_t t0 = t * kStrTile, t1 = (v.n < t0 + kStrTile ? v.n : t0 + kStrTile);
+        const uint64_t r0 = t0 + uint64_t(threadIdx.x) * kPackRow;
+        const uint32_t rows = r0 >= t1 ? 0u : (t1 - r0 < kPackRow ? uint32_t(t1 - r0) : uint32_t(kPackRow));
+        uint64_t       loc[kPackRow];
+#pragma unroll
+        for (int k = 0; k < kPackRow; ++k) loc[k] = uint32_t(k) < rows ? v.ol[r0 + k] : 0;
+        TileCosts c = row_costs(loc, rows);
+        tile_max_any(c.maxc, c.greedy, sm);
+        PageDesc* desc = v.desc + v.tile_off[t];
+        if (c.greedy) {
+            if (threadIdx.x < 32) pack_tile(v.ol, v.base, v.npages, t0, t1, desc);
+            __syncthreads();
+            continue;
+        }
+        const uint64_t T = kCap - c.maxc;
+        // exclusive prefix of (non-NULL rows << 40 | string bytes) at this thread's first row
+        uint64_t       tot;
+        const uint64_t pre = block_exclusive_scan<uint64_t>((uint64_t(c.nn) << 40) | c.len, s_scan, &tot);
+        const uint32_t li0 = uint32_t(r0 - t0);
+        uint32_t       NN = uint32_t(pre >> 40), LEN = uint32_t(pre & ((1ull << 40) - 1));
+        // S: the row's start in eighths of a byte (offsets, string bytes, one bit per row)
+        uint64_t S = 8ull * (2ull * NN + LEN) + li0;
+        // start of the row before this thread's first row (the previous thread's last row)
+        uint64_t S_prev = li0 > 0 && rows > 0 ? S - loc_cost(v.ol[r0 - 1]) : 0;
+#pragma unroll
+        for (int k = 0; k < kPackRow; ++k) {
+            if (uint32_t(k) >= rows) break;
+            const uint32_t li = li0 + k;
+            const uint64_t pg = S / T;
+            if ((li == 0 || S_prev / T != pg) && pg < uint64_t(kMaxTilePages)) {  // first row of its page
+                p_row[pg] = uint16_t(li);
+                p_nn[pg]  = uint16_t(NN);
+                p_len[pg] = LEN;
+            }
+            if (uint64_t(li) + 1 == t1 - t0) s_np = uint32_t(pg) + 1;
+            NN += loc[k] != 0;
+            LEN += loc[k] != 0 ? uint32_t(loc_len_field(loc[k])) : 0u;
+            S_prev = S;
+            S += c.cost[k];
+        }
+        __syncthreads();
+        const uint32_t np = s_np < uint32_t(kMaxTilePages) ? s_np : uint32_t(kMaxTilePages);
+        const uint32_t nt = uint32_t(tot >> 40), lt = uint32_t(tot & ((1ull << 40) - 1));
+        for (uint32_t p = threadIdx.x; p < np; p += blockDim.x) {
+            const uint32_t rs = p_row[p], re = p + 1 < np ? p_row[p + 1] : uint32_t(t1 - t0);
+            const uint32_t ns = p_nn[p], ne = p + 1 < np ? p_nn[p + 1] : nt;
+            const uint32_t ls = p_len[p], le = p + 1 < np ? p_len[p + 1] : lt;
+            desc[p] = PageDesc{t0 + rs, re - rs, ne - ns, le - ls, 0};
+        }
+        __syncthreads();
+    }
 }
 
 // Copies `len` bytes of a normal string from global `src` (inside an input
@@ -397,7 +551,7 @@ void varchar_plan(std::vector<VarcharOut*>& vs, cudaStream_t st) {
         v.tile_off   = dalloc_n<uint64_t>(v.ntiles + 1, st);
     }
     for_pack_groups(vs, [&](const PackCols& P, uint64_t tiles) {
-        k_pack_count<<<div_up(tiles * 32, 128), 128, 0, st>>>(P, tiles);
+        k_pack_count<<<grid_of(tiles, 4), kPackT, 0, st>>>(P, tiles);
         HJ_LAUNCH_CHECK();
     });
     for (auto* vp : vs)
@@ -410,7 +564,7 @@ std::vector<uint8_t*> varchar_write(std::vector<VarcharOut*>& vs, const std::vec
     for (size_t i = 0; i < vs.size(); ++i)
         if (vs[i]->n) vs[i]->desc = static_cast<PageDesc*>(dalloc(std::max<uint64_t>(pages[i], 1) * sizeof(PageDesc), st));
     for_pack_groups(vs, [&](const PackCols& P, uint64_t tiles) {
-        k_pack_emit<<<div_up(tiles * 32, 128), 128, 0, st>>>(P, tiles);
+        k_pack_emit<<<grid_of(tiles, 4), kPackT, 0, st>>>(P, tiles);
         HJ_LAUNCH_CHECK();
     });
     for (size_t i = 0; i < vs.size(); ++i) {

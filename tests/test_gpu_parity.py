@@ -234,3 +234,43 @@ def test_table_probe_pairs(engine, hj, orc):
         assert np.unique(pr.astype(np.int64) << 32 | br).size == pr.size   # no duplicates
     finally:
         L.hj_table_free(t)
+
+
+def _varchar_pages_fit(pages):
+    """Every normal VARCHAR page fits (header, offsets, bytes, bitmap) with
+    non-decreasing offsets; returns the number of normal pages."""
+    normal = 0
+    for pg in pages:
+        h = pg[:4].view(np.uint16)
+        rows, nn = int(h[0]), int(h[1])
+        if rows in (0xFFFF, 0xFFFE):
+            continue
+        normal += 1
+        offs = pg[4:4 + 2 * nn].view(np.uint16).astype(np.int64)
+        assert nn <= rows and np.all(np.diff(offs) >= 0)
+        end = int(offs[-1]) if nn else 0
+        assert 4 + 2 * nn + end + (rows + 7) // 8 <= 8192
+    return normal
+
+
+def test_varchar_page_packing_both_rules(engine, orc, hj):
+    """Output VARCHAR pages are packed per 4096-row tile by prefix sums (short
+    strings) or by the greedy rule (a tile with a string over ~1 KB or a long
+    string).  Both give the oracle's rows, every page fits, and the prefix-sum
+    tiles use at most ~1% more pages than a greedy packing."""
+    r = np.random.default_rng(5)
+    n = 5 * 4096 + 77
+    strs = [None if r.random() < 0.15 else "v" * int(r.integers(0, 65)) for _ in range(n)]
+    strs[4096 + 10] = "K" * 2000          # tile 1: a row over kCap / 8 -> greedy
+    strs[3 * 4096 + 5] = "L" * 9000       # tile 3: a long string -> greedy
+    keys = list(range(n))
+    build = cases.table(hj, [[k, s] for k, s in zip(keys, strs)], [cases.I, cases.V])
+    probe = cases.table(hj, [[k] for k in keys], [cases.I])
+    p = hj.Plan()
+    cases._two_scans(hj, p, build, probe, [(0, cases.I), (1, cases.V)], [(0, cases.I)])
+    p.root = p.new_join_node(True, 0, 1, 0, 0, [(1, cases.V), (2, cases.I)])
+    res = engine.execute(p)
+    assert_same(orc, res, orc.run(orc.port(), p), "varchar packing")
+    normal = _varchar_pages_fit(res.columns[0].pages)
+    bytes_ = sum(2 + len(s) for s in strs if s is not None and len(s) <= 8185) + n / 8
+    assert normal <= bytes_ / 8000 + 6 * 2
