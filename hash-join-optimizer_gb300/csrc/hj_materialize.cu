@@ -440,21 +440,29 @@ __device__ __forceinline__ void copy_string(uint8_t* img, uint32_t dst, const ui
     }
 }
 
-__global__ void __launch_bounds__(kMT)
+// One warp per output page, assembled in the warp's own 8 KB of shared memory
+// (no block barriers): 32-row chunks, a warp scan of (non-NULL, bytes) per
+// chunk, one string per lane, then the image is stored with 16-byte writes.
+constexpr int kVW = 8;  // warps (pages in flight) per block
+
+__global__ void __launch_bounds__(kVW * 32)
     k_write_varchar_pages(const PageDesc* __restrict__ desc, uint64_t ndesc, const uint64_t* __restrict__ ol,
                           const uint8_t* __restrict__ base, uint64_t npages, uint8_t* __restrict__ out) {
-    __shared__ __align__(16) uint8_t img[kPage];
-    __shared__ uint32_t              sm[33];
-    for (uint64_t pi = blockIdx.x; pi < ndesc; pi += gridDim.x) {
+    extern __shared__ __align__(16) uint8_t vimg[];
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint8_t*       img  = vimg + size_t(warp) * kPage;
+    uint4*         w4   = reinterpret_cast<uint4*>(img);
+    for (uint64_t pi = uint64_t(blockIdx.x) * kVW + warp; pi < ndesc; pi += uint64_t(gridDim.x) * kVW) {
         const PageDesc d = desc[pi];
-        zero_img(img);
-        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < kPage / 16 / 32; ++k) w4[lane + 32 * k] = make_uint4(0, 0, 0, 0);
+        __syncwarp();
         if (d.count == 0) {  // long-string page `chunk` of the string in row d.row
             const uint64_t loc = ol[d.row];
             const uint32_t L   = loc_len(loc, base, npages);
             const uint32_t beg = d.chunk * kLongChunk;
             const uint32_t len = min(kLongChunk, L - beg);
-            if (threadIdx.x == 0) {
+            if (lane == 0) {
                 *reinterpret_cast<uint16_t*>(img)     = d.chunk == 0 ? 0xffff : 0xfffe;
                 *reinterpret_cast<uint16_t*>(img + 2) = uint16_t(len);
             }
@@ -465,25 +473,27 @@ __global__ void __launch_bounds__(kMT)
                 const uint8_t* pg = base + q * kPage;
                 const uint32_t pl = *reinterpret_cast<const uint16_t*>(pg + 2);
                 const uint32_t lo = max(so, beg), hi = min(so + pl, beg + len);
-                for (uint32_t x = lo + threadIdx.x; x < hi; x += blockDim.x) img[4 + x - beg] = pg[4 + x - so];
+                for (uint32_t x = lo + lane; x < hi; x += 32) img[4 + x - beg] = pg[4 + x - so];
                 so += pl;
             }
         } else {
             const uint32_t data0  = 4 + 2 * d.nn;
             const uint32_t nbytes = (d.count + 7) / 8, bm0 = kPage - nbytes;
             uint32_t       rank0 = 0, byte0 = 0;
-            for (uint32_t c = 0; c < d.count; c += blockDim.x) {
-                const uint32_t i   = c + threadIdx.x;
-                const uint64_t loc = i < d.count ? ol[d.row + i] : 0;
+            uint64_t       next  = lane < d.count ? ol[d.row + lane] : 0;
+            for (uint32_t c = 0; c < d.count; c += 32) {
+                const uint64_t loc = next;
+                next               = c + 32 + lane < d.count ? ol[d.row + c + 32 + lane] : 0;
                 const bool     on  = loc != 0;
                 const uint32_t len = on ? uint32_t(loc_len_field(loc)) : 0u;
-                // one scan of (non-NULL count << 16 | bytes): a chunk holds at most
-                // 256 rows and a page at most 8188 bytes, so neither half overflows
-                uint32_t       tot;
-                const uint32_t ex   = block_exclusive_scan<uint32_t>((on ? 0x10000u : 0u) | len, sm, &tot);
+                // (non-NULL count << 16 | bytes): a page holds at most 8188 string
+                // bytes, so the low half never carries into the high one
+                const uint32_t v    = (on ? 0x10000u : 0u) | len;
+                const uint32_t inc  = warp_inclusive_scan<uint32_t>(v);
+                const uint32_t tot  = __shfl_sync(0xffffffffu, inc, 31);
+                const uint32_t ex   = inc - v;
                 const uint32_t rank = rank0 + (ex >> 16);
                 const uint32_t boff = byte0 + (ex & 0xffffu);
-                const uint32_t tr = tot >> 16, tb = tot & 0xffffu;
                 // the packer guarantees both bounds; they are checked so that no
                 // inconsistent descriptor can write outside the page image
                 if (on && rank < d.nn && data0 + boff + len <= bm0) {
@@ -491,18 +501,20 @@ __global__ void __launch_bounds__(kMT)
                     copy_string(img, data0 + boff, base + loc_off(loc), len);
                 }
                 const uint32_t b = __ballot_sync(0xffffffffu, on);
-                if ((threadIdx.x & 31) == 0) put_bits(img, bm0, nbytes, c + (threadIdx.x & ~31u), b);
-                rank0 += tr;
-                byte0 += tb;
+                if (lane == 0) put_bits(img, bm0, nbytes, c, b);
+                rank0 += tot >> 16;
+                byte0 += tot & 0xffffu;
             }
-            if (threadIdx.x == 0) {
+            if (lane == 0) {
                 *reinterpret_cast<uint16_t*>(img)     = uint16_t(d.count);
                 *reinterpret_cast<uint16_t*>(img + 2) = uint16_t(d.nn);
             }
         }
-        __syncthreads();
-        store_page(out + pi * kPage, img);
-        __syncthreads();
+        __syncwarp();
+        uint4* dst = reinterpret_cast<uint4*>(out + pi * kPage);
+#pragma unroll
+        for (int k = 0; k < kPage / 16 / 32; ++k) dst[lane + 32 * k] = w4[lane + 32 * k];
+        __syncwarp();
     }
 }
 
@@ -571,8 +583,10 @@ std::vector<uint8_t*> varchar_write(std::vector<VarcharOut*>& vs, const std::vec
         VarcharOut& v = *vs[i];
         if (v.n == 0) continue;
         out[i] = static_cast<uint8_t*>(dalloc(std::max<uint64_t>(pages[i], 1) * kPage, st));
-        k_write_varchar_pages<<<grid_of(pages[i]), kMT, 0, st>>>(v.desc, pages[i], v.ol, v.base, v.base_pages,
-                                                                 out[i]);
+        HJ_CUDA(cudaFuncSetAttribute(k_write_varchar_pages, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     kVW * kPage));
+        k_write_varchar_pages<<<grid_of(div_up(pages[i], kVW), 3), kVW * 32, kVW * kPage, st>>>(
+            v.desc, pages[i], v.ol, v.base, v.base_pages, out[i]);
         HJ_LAUNCH_CHECK();
         for (void* p : {(void*)v.desc, (void*)v.ol, (void*)v.tile_pages, (void*)v.tile_off}) dfree(p, st);
         v.desc       = nullptr;
