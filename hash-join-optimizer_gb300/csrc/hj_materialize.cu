@@ -64,6 +64,12 @@ __device__ __forceinline__ void put_bits(uint8_t* img, uint32_t bm0, uint32_t nb
 
 // ---- INT32 -----------------------------------------------------------------
 
+// Block per output page of 1984 rows: thread t takes rows 8t .. 8t+7, issues
+// their 8 gathers together, and owns bitmap byte t; one block scan of the
+// non-NULL counts places the values.
+constexpr int kIntRows = 8;
+static_assert(kMT * kIntRows >= kDenseRows, "one pass per page");
+
 __global__ void __launch_bounds__(kMT)
     k_write_int32_pages(IntCol col, const uint32_t* __restrict__ rid, uint64_t n, uint8_t* __restrict__ out) {
     __shared__ __align__(16) uint8_t img[kPage];
@@ -75,28 +81,34 @@ __global__ void __launch_bounds__(kMT)
         const uint64_t r0 = p * kDenseRows;
         const uint32_t nr = uint32_t(n - r0 < uint64_t(kDenseRows) ? n - r0 : uint64_t(kDenseRows));
         zero_img(img);
-        __syncthreads();
-        const uint32_t nbytes = (nr + 7) / 8, bm0 = kPage - nbytes;
-        uint32_t       nn     = 0;
-        for (uint32_t c = 0; c < nr; c += blockDim.x) {
-            const uint32_t i  = c + threadIdx.x;
-            bool           on = false;
-            int32_t        v  = 0;
-            if (i < nr) on = int_get(col, rid ? uint64_t(__ldg(rid + r0 + i)) : r0 + i, v);
-            uint32_t tot, rank;
-            if (nullable) {
-                rank = block_exclusive_scan<uint32_t>(on ? 1u : 0u, sm, &tot);
-            } else {
-                rank = threadIdx.x;
-                tot  = min(nr - c, uint32_t(blockDim.x));
-            }
-            if (on) words[1 + nn + rank] = uint32_t(v);
-            const uint32_t b = __ballot_sync(0xffffffffu, on);
-            if ((threadIdx.x & 31) == 0) put_bits(img, bm0, nbytes, c + (threadIdx.x & ~31u), b);
-            nn += tot;
+        const uint32_t i0 = threadIdx.x * kIntRows;
+        uint32_t       row[kIntRows];
+#pragma unroll
+        for (int k = 0; k < kIntRows; ++k) {
+            const uint32_t i = i0 + k;
+            row[k]           = i < nr ? (rid ? __ldg(rid + r0 + i) : uint32_t(r0 + i)) : 0u;
         }
-        __syncthreads();
-        if (threadIdx.x == 0) words[0] = nr | (nn << 16);
+        int32_t  v[kIntRows];
+        uint32_t on = 0;
+#pragma unroll
+        for (int k = 0; k < kIntRows; ++k) {
+            v[k] = 0;
+            if (i0 + k < nr && int_get(col, row[k], v[k])) on |= 1u << k;
+        }
+        uint32_t tot;
+        const uint32_t rank = nullable ? block_exclusive_scan<uint32_t>(__popc(on), sm, &tot)
+                                       : (i0 < nr ? i0 : nr);
+        if (!nullable) {
+            tot = nr;
+            __syncthreads();  // the image is zeroed
+        }
+        uint32_t q = rank;
+#pragma unroll
+        for (int k = 0; k < kIntRows; ++k)
+            if ((on >> k) & 1u) words[1 + q++] = uint32_t(v[k]);
+        const uint32_t nbytes = (nr + 7) / 8;
+        if (i0 < nr) img[kPage - nbytes + threadIdx.x] = uint8_t(on);
+        if (threadIdx.x == 0) words[0] = nr | (tot << 16);
         __syncthreads();
         store_page(out + p * kPage, img);
         __syncthreads();
