@@ -33,7 +33,7 @@
 namespace hj {
 namespace {
 
-constexpr int kLocalBits   = 13;  // buckets per partition = 2^13 (64 KB of shared counters)
+constexpr int kLocalBits   = 12;  // buckets per partition = 2^12 (16 KB of shared counters)
 constexpr int kMaxRadix    = 14;
 constexpr int kThreads     = 512;
 constexpr int kItems       = 16;
@@ -141,6 +141,14 @@ __global__ void __launch_bounds__(kThreads)
     }
 }
 
+// Partitions of at most kFuseMax tuples are built by one block each
+// (k_bucket_local); the chunked kernels take the larger ones.
+constexpr uint32_t kFuseMax = 12288;
+
+__device__ __forceinline__ bool fused_part(const uint32_t* part_off, uint32_t part) {
+    return part_off[part + 1] - part_off[part] <= kFuseMax;
+}
+
 // Locates chunk `cid`: its partition and tuple range.  Returns false past the end.
 __device__ __forceinline__ bool chunk_range(uint32_t cid, const uint32_t* chunk_off,
                                             const uint32_t* part_off, uint32_t P, uint32_t& part,
@@ -189,6 +197,7 @@ __global__ void __launch_bounds__(kThreads)
     uint32_t       part, s, e;
     bool           single;
     if (!chunk_range(blockIdx.x, chunk_off, part_off, 1u << g.R, part, s, e, single)) return;
+    if (fused_part(part_off, part)) return;  // k_bucket_local
     for (uint32_t i = threadIdx.x; i < 2 * nl; i += blockDim.x) sh[i] = 0;
     __syncthreads();
     const uint32_t lmask = nl - 1;
@@ -226,6 +235,7 @@ __global__ void __launch_bounds__(1024)
     const uint64_t gb   = uint64_t(part) << g.L;
     const uint32_t P    = 1u << g.R;
     uint32_t       run  = part_off[part];
+    if (fused_part(part_off, part)) return;  // k_bucket_local (also writes the sentinel word)
     if (part_off[part + 1] == run) {  // empty partition: all buckets empty
         for (uint32_t i = threadIdx.x; i < nl; i += blockDim.x) {
             dir[gb + i]  = uint64_t(run) << 16;
@@ -245,7 +255,6 @@ __global__ void __launch_bounds__(1024)
             run += tot;
         }
     }
-    if (part == P - 1 && threadIdx.x == 0) dir[uint64_t(P) << g.L] = uint64_t(part_off[P]) << 16;
 }
 
 // 6. Final scatter into bucket order.
@@ -259,6 +268,7 @@ __global__ void __launch_bounds__(kThreads, 2)
     uint32_t       part, s, e;
     bool           single;
     if (!chunk_range(blockIdx.x, chunk_off, part_off, 1u << g.R, part, s, e, single)) return;
+    if (fused_part(part_off, part)) return;  // k_bucket_local
     for (uint32_t i = threadIdx.x; i < nl; i += blockDim.x) sh[i] = 0;
     __syncthreads();
     const uint32_t lmask = nl - 1;
@@ -292,13 +302,122 @@ __global__ void __launch_bounds__(kThreads, 2)
     }
 }
 
+// 4-7 in one block for a partition of at most kFuseMax tuples: bucket counts
+// and Bloom tags in shared memory, the directory words from one scan of the
+// counts, then the tuples placed in bucket order in shared memory and stored
+// with coalesced writes (scattered 4-byte stores would cost one L2 request
+// each); the mixed bits come from neighbouring keys of the placed order.
+// Larger partitions (Zipf-heavy keys) take the chunked kernels, which skip the
+// partitions handled here.
+constexpr int kLT = 1024;  // threads of k_bucket_local
+
+__global__ void __launch_bounds__(kLT, 1)
+    k_bucket_local(Geo g, const uint32_t* __restrict__ part_off, const int32_t* __restrict__ tkey,
+                   const uint32_t* __restrict__ trow, uint64_t* __restrict__ dir, int32_t* __restrict__ okey,
+                   uint32_t* __restrict__ orow, uint32_t* __restrict__ mixed) {
+    extern __shared__ uint32_t sh[];
+    __shared__ uint32_t wsum[kLT / 32];
+    const uint32_t nl    = 1u << g.L;
+    const uint32_t lmask = nl - 1;
+    const uint32_t P     = 1u << g.R;
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t nbw = (nl + 1) / 2, nmw = (nl + 31) / 32;
+    uint32_t* cnt = sh;                 // nl: counts, then cursors
+    uint32_t* blm = sh + nl;            // nbw words: two 16-bit Bloom tags each
+    uint32_t* mix = sh + nl + nbw;      // nmw words of mixed bits
+    int32_t*  sk  = reinterpret_cast<int32_t*>(mix + nmw);  // kFuseMax staged keys
+    uint32_t* sr  = reinterpret_cast<uint32_t*>(sk + kFuseMax);        // and rows
+    if (blockIdx.x == 0 && threadIdx.x == 0) dir[uint64_t(P) << g.L] = uint64_t(part_off[P]) << 16;
+    for (uint32_t part = blockIdx.x; part < P; part += gridDim.x) {
+        if (!fused_part(part_off, part)) continue;
+        const uint32_t s = part_off[part], e = part_off[part + 1];
+        const uint64_t gb = uint64_t(part) << g.L;
+        for (uint32_t i = threadIdx.x; i < nl + nbw + nmw; i += blockDim.x) sh[i] = 0;
+        __syncthreads();
+        // counts and Bloom tags
+        for (uint32_t w0 = s + (threadIdx.x & ~31u); w0 < e; w0 += blockDim.x) {
+            const uint32_t j   = w0 + lane;
+            const bool     ok  = j < e;
+            const unsigned act = __ballot_sync(0xffffffffu, ok);
+            if (ok) {
+                const uint64_t h     = fib_hash(tkey[j]);
+                const uint32_t local = uint32_t(bucket_of(h, g.b)) & lmask;
+                bucket_add(cnt, local, act);
+                atomicOr(blm + (local >> 1), bloom_mask(h) << (16 * (local & 1)));
+            }
+        }
+        __syncthreads();
+        // exclusive scan of the counts: warp w scans segments of 32 counts
+        // (lane i reads count 32 q + i: no bank conflicts), then the warps' totals
+        const uint32_t nseg = (nl + 31) / 32, per_w = (nseg + kLT / 32 - 1) / (kLT / 32);
+        uint32_t       wrun = 0;
+        for (uint32_t q = warp * per_w; q < min(nseg, (warp + 1) * per_w); ++q) {
+            const uint32_t i = 32 * q + lane;
+            const uint32_t c = i < nl ? cnt[i] : 0u;
+            wrun += warp_sum(c);
+        }
+        if (lane == 0) wsum[warp] = wrun;
+        __syncthreads();
+        uint32_t base = s;
+        for (uint32_t w = 0; w < warp; ++w) base += wsum[w];
+        for (uint32_t q = warp * per_w; q < min(nseg, (warp + 1) * per_w); ++q) {
+            const uint32_t i   = 32 * q + lane;
+            const uint32_t c   = i < nl ? cnt[i] : 0u;
+            const uint32_t inc = warp_inclusive_scan(c);
+            if (i < nl) {
+                const uint32_t start = base + inc - c;
+                cnt[i]               = start;
+                dir[gb + i]          = (uint64_t(start) << 16) | ((blm[i >> 1] >> (16 * (i & 1))) & 0xffffu);
+            }
+            base += __shfl_sync(0xffffffffu, inc, 31);
+        }
+        __syncthreads();
+        // place the tuples in bucket order
+        for (uint32_t w0 = s + (threadIdx.x & ~31u); w0 < e; w0 += blockDim.x) {
+            const uint32_t j   = w0 + lane;
+            const bool     ok  = j < e;
+            const unsigned act = __ballot_sync(0xffffffffu, ok);
+            if (ok) {
+                const int32_t  k     = tkey[j];
+                const uint32_t local = uint32_t(bucket_of(fib_hash(k), g.b)) & lmask;
+                const uint32_t q     = bucket_add(cnt, local, act) - s;
+                sk[q]                = k;
+                sr[q]                = trow[j];
+            }
+        }
+        __syncthreads();
+        // coalesced stores; a bucket is mixed when two neighbours in it differ
+        for (uint32_t q = threadIdx.x; q < e - s; q += blockDim.x) {
+            const int32_t k = sk[q];
+            okey[s + q]     = k;
+            orow[s + q]     = sr[q];
+            if (q > 0 && sk[q - 1] != k) {
+                const uint32_t local = uint32_t(bucket_of(fib_hash(k), g.b)) & lmask;
+                if ((uint32_t(bucket_of(fib_hash(sk[q - 1]), g.b)) & lmask) == local)
+                    atomicOr(mix + (local >> 5), 1u << (local & 31));
+            }
+        }
+        __syncthreads();
+        // the partition's buckets are whole mixed words (2^L >= 32) or share one
+        if (nl >= 32) {
+            for (uint32_t i = threadIdx.x; i < nl / 32; i += blockDim.x) mixed[(gb >> 5) + i] = mix[i];
+        } else if (threadIdx.x == 0 && mix[0]) {
+            atomicOr(mixed + (gb >> 5), mix[0] << (gb & 31));
+        }
+        __syncthreads();
+    }
+}
+
 // 7. mixed[p] bit set when bucket p holds two different keys.
-__global__ void k_bucket_mixed(uint32_t b, uint64_t n, const uint64_t* __restrict__ dir,
-                               const int32_t* __restrict__ key, uint32_t* __restrict__ mixed) {
+__global__ void k_bucket_mixed(Geo g, uint64_t n, const uint32_t* __restrict__ part_off,
+                               const uint64_t* __restrict__ dir, const int32_t* __restrict__ key,
+                               uint32_t* __restrict__ mixed) {
+    const uint32_t b      = g.b;
     const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
     for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < n; j += stride) {
         const int32_t  k     = key[j];
         const uint64_t p     = bucket_of(fib_hash(k), b);
+        if (fused_part(part_off, uint32_t(p >> g.L))) continue;  // set by k_bucket_local
         const uint64_t first = __ldg(dir + p) >> 16;
         if (key[first] != k) atomicOr(mixed + (p >> 5), 1u << (p & 31));
     }
@@ -341,6 +460,7 @@ void build_table(const KeyCol& kc, int dir_bits, int radix_bits, Table& t, uint6
     prefer_shared(k_part_scatter);
     prefer_shared(k_bucket_count);
     prefer_shared(k_bucket_scatter);
+    prefer_shared(k_bucket_local);
     unsigned long long* d_nvalid = dalloc_n<unsigned long long>(1, st);
     uint32_t*           part_cnt = nullptr;
     auto run_hist = [&](uint32_t r) {
@@ -418,6 +538,14 @@ void build_table(const KeyCol& kc, int dir_bits, int radix_bits, Table& t, uint6
     k_bucket_dir<<<P, 1024, 0, st>>>(g, part_off, gcnt, gbloom, t.dir);
     HJ_LAUNCH_CHECK();
     {
+        const size_t nl   = size_t(1) << g.L;
+        const size_t smem = (nl + (nl + 1) / 2 + (nl + 31) / 32 + 2 * size_t(kFuseMax)) * sizeof(uint32_t);
+        HJ_CUDA(cudaFuncSetAttribute(k_bucket_local, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+        k_bucket_local<<<std::min<uint32_t>(P, uint32_t(kSMs)), kLT, smem, st>>>(g, part_off, tkey, trow, t.dir,
+                                                                                t.keys, t.rows, t.mixed);
+        HJ_LAUNCH_CHECK();
+    }
+    {
         const size_t smem = (size_t(1) << g.L) * sizeof(uint32_t);
         HJ_CUDA(cudaFuncSetAttribute(k_bucket_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      int(smem)));
@@ -425,7 +553,7 @@ void build_table(const KeyCol& kc, int dir_bits, int radix_bits, Table& t, uint6
                                                               t.keys, t.rows);
         HJ_LAUNCH_CHECK();
     }
-    k_bucket_mixed<<<grid_for(nv, 256, 8), 256, 0, st>>>(b, nv, t.dir, t.keys, t.mixed);
+    k_bucket_mixed<<<grid_for(nv, 256, 8), 256, 0, st>>>(g, nv, part_off, t.dir, t.keys, t.mixed);
     HJ_LAUNCH_CHECK();
 
     for (void* p : {(void*)d_nvalid, (void*)part_cnt, (void*)part_off, (void*)part_cursor,
