@@ -105,39 +105,75 @@ __global__ void __launch_bounds__(1024)
 }
 
 // 3. Scatter (key, row) to partitions.  Each block owns a tile of kTile rows:
-//    one global atomic per (tile, non-empty partition) reserves its space.
-__global__ void __launch_bounds__(kThreads)
+//    shared-memory counts give every item its rank in its partition within
+//    the tile, one global atomic per (tile, non-empty partition) reserves the
+//    partition's space, the items are placed partition by partition in shared
+//    memory and then stored so that consecutive threads write consecutive
+//    slots of a partition (runs instead of single 4-byte stores).
+__global__ void __launch_bounds__(kThreads, 2)
     k_part_scatter(KeyCol kc, uint32_t R, uint32_t* __restrict__ part_cursor,
                    int32_t* __restrict__ tkey, uint32_t* __restrict__ trow) {
-    extern __shared__ uint32_t sh[];  // P counters, reused as bases
+    extern __shared__ uint32_t sh[];  // P counters / tile offsets, P global bases, staged items
+    __shared__ uint32_t sm[33];
     const uint32_t P     = 1u << R;
+    uint32_t*      off   = sh;                   // counts, then the tile's partition offsets
+    uint32_t*      gbase = sh + P;               // global slot of each partition's first item
+    int32_t*       sk    = reinterpret_cast<int32_t*>(sh + 2 * P);
+    uint32_t*      sr    = sh + 2 * P + kTile;
+    uint16_t*      sp    = reinterpret_cast<uint16_t*>(sh + 2 * P + 2 * kTile);  // partition of each slot
     const uint64_t tile0 = uint64_t(blockIdx.x) * kTile;
-    for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) sh[i] = 0;
+    for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) off[i] = 0;
     __syncthreads();
     int32_t  keys[kItems];
-    uint32_t parts[kItems];
+    uint32_t parts[kItems], rank[kItems];
     uint32_t okmask = 0;
 #pragma unroll
     for (int k = 0; k < kItems; ++k) {
         const uint64_t i  = tile0 + uint64_t(k) * kThreads + threadIdx.x;
         const bool     ok = load_key(kc, i, keys[k]);
         parts[k]          = ok ? uint32_t(bucket_of(fib_hash(keys[k]), R)) : 0;
-        if (ok) {
-            atomicAdd(sh + parts[k], 1u);
-            okmask |= 1u << k;
-        }
+        rank[k]           = ok ? atomicAdd(off + parts[k], 1u) : 0;
+        okmask |= uint32_t(ok) << k;
     }
     __syncthreads();
-    for (uint32_t i = threadIdx.x; i < P; i += blockDim.x)
-        if (sh[i]) sh[i] = atomicAdd(part_cursor + i, sh[i]);
+    // exclusive scan of the counts (thread t: partitions [t * per, (t + 1) * per))
+    const uint32_t per = (P + kThreads - 1) / kThreads;
+    uint32_t       run = 0;
+    for (uint32_t q = 0; q < per; ++q) {
+        const uint32_t p = threadIdx.x * per + q;
+        if (p < P) {
+            const uint32_t c = off[p];
+            gbase[p]         = c ? atomicAdd(part_cursor + p, c) : 0u;
+            run += c;
+        }
+    }
+    uint32_t       tot;
+    const uint32_t ex = block_exclusive_scan<uint32_t>(run, sm, &tot);
+    run               = ex;
+    for (uint32_t q = 0; q < per; ++q) {
+        const uint32_t p = threadIdx.x * per + q;
+        if (p < P) {
+            const uint32_t c = off[p];
+            off[p]           = run;
+            run += c;
+        }
+    }
     __syncthreads();
 #pragma unroll
     for (int k = 0; k < kItems; ++k) {
         if ((okmask >> k) & 1u) {
-            const uint32_t pos = atomicAdd(sh + parts[k], 1u);
-            tkey[pos]          = keys[k];
-            trow[pos]          = uint32_t(tile0 + uint64_t(k) * kThreads + threadIdx.x);
+            const uint32_t q = off[parts[k]] + rank[k];
+            sk[q]            = keys[k];
+            sr[q]            = uint32_t(tile0 + uint64_t(k) * kThreads + threadIdx.x);
+            sp[q]            = uint16_t(parts[k]);
         }
+    }
+    __syncthreads();
+    for (uint32_t q = threadIdx.x; q < tot; q += blockDim.x) {
+        const uint32_t p   = sp[q];
+        const uint32_t pos = gbase[p] + (q - off[p]);
+        tkey[pos]          = sk[q];
+        trow[pos]          = sr[q];
     }
 }
 
@@ -408,16 +444,18 @@ __global__ void __launch_bounds__(kLT, 1)
     }
 }
 
-// 7. mixed[p] bit set when bucket p holds two different keys.
-__global__ void k_bucket_mixed(Geo g, uint64_t n, const uint32_t* __restrict__ part_off,
-                               const uint64_t* __restrict__ dir, const int32_t* __restrict__ key,
-                               uint32_t* __restrict__ mixed) {
-    const uint32_t b      = g.b;
-    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
-    for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < n; j += stride) {
+// 7. mixed[p] bit set when bucket p holds two different keys (chunks of the
+//    partitions k_bucket_local does not take).
+__global__ void __launch_bounds__(kThreads)
+    k_bucket_mixed(Geo g, const uint32_t* __restrict__ chunk_off, const uint32_t* __restrict__ part_off,
+                   const uint64_t* __restrict__ dir, const int32_t* __restrict__ key, uint32_t* __restrict__ mixed) {
+    uint32_t part, s, e;
+    bool     single;
+    if (!chunk_range(blockIdx.x, chunk_off, part_off, 1u << g.R, part, s, e, single)) return;
+    if (fused_part(part_off, part)) return;  // set by k_bucket_local
+    for (uint32_t j = s + threadIdx.x; j < e; j += blockDim.x) {
         const int32_t  k     = key[j];
-        const uint64_t p     = bucket_of(fib_hash(k), b);
-        if (fused_part(part_off, uint32_t(p >> g.L))) continue;  // set by k_bucket_local
+        const uint64_t p     = bucket_of(fib_hash(k), g.b);
         const uint64_t first = __ldg(dir + p) >> 16;
         if (key[first] != k) atomicOr(mixed + (p >> 5), 1u << (p & 31));
     }
@@ -506,10 +544,8 @@ void build_table(const KeyCol& kc, int dir_bits, int radix_bits, Table& t, uint6
     int32_t*  tkey = dalloc_n<int32_t>(nv, st);
     uint32_t* trow = dalloc_n<uint32_t>(nv, st);
     {
-        const size_t smem = P * sizeof(uint32_t);
-        if (smem > 48 * 1024)
-            HJ_CUDA(cudaFuncSetAttribute(k_part_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         int(smem)));
+        const size_t smem = (2 * size_t(P) + 2 * size_t(kTile)) * sizeof(uint32_t) + kTile * sizeof(uint16_t);
+        HJ_CUDA(cudaFuncSetAttribute(k_part_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
         k_part_scatter<<<div_up(kc.n, kTile), kThreads, smem, st>>>(kc, R, part_cursor, tkey, trow);
         HJ_LAUNCH_CHECK();
     }
@@ -553,7 +589,7 @@ void build_table(const KeyCol& kc, int dir_bits, int radix_bits, Table& t, uint6
                                                               t.keys, t.rows);
         HJ_LAUNCH_CHECK();
     }
-    k_bucket_mixed<<<grid_for(nv, 256, 8), 256, 0, st>>>(g, nv, part_off, t.dir, t.keys, t.mixed);
+    k_bucket_mixed<<<chunks_upper, kThreads, 0, st>>>(g, chunk_off, part_off, t.dir, t.keys, t.mixed);
     HJ_LAUNCH_CHECK();
 
     for (void* p : {(void*)d_nvalid, (void*)part_cnt, (void*)part_off, (void*)part_cursor,
