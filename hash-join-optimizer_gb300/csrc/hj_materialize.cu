@@ -357,22 +357,24 @@ __global__ void __launch_bounds__(kPackT) k_pack_emit(PackCols P, uint64_t ntile
             __syncthreads();
             continue;
         }
-        const uint64_t T = kCap - c.maxc;
+        // S stays below 2^32: at most 4096 rows of at most kCap / 8 eighths each
+        const uint32_t T = kCap - c.maxc;
         // exclusive prefix of (non-NULL rows << 40 | string bytes) at this thread's first row
         uint64_t       tot;
         const uint64_t pre = block_exclusive_scan<uint64_t>((uint64_t(c.nn) << 40) | c.len, s_scan, &tot);
         const uint32_t li0 = uint32_t(r0 - t0);
         uint32_t       NN = uint32_t(pre >> 40), LEN = uint32_t(pre & ((1ull << 40) - 1));
         // S: the row's start in eighths of a byte (offsets, string bytes, one bit per row)
-        uint64_t S = 8ull * (2ull * NN + LEN) + li0;
+        uint32_t S = 8u * (2u * NN + LEN) + li0;
         // start of the row before this thread's first row (the previous thread's last row)
-        uint64_t S_prev = li0 > 0 && rows > 0 ? S - loc_cost(v.ol[r0 - 1]) : 0;
+        uint32_t S_prev = li0 > 0 && rows > 0 ? S - loc_cost(v.ol[r0 - 1]) : 0u;
+        uint32_t pg_prev = S_prev / T;
 #pragma unroll
         for (int k = 0; k < kPackRow; ++k) {
             if (uint32_t(k) >= rows) break;
             const uint32_t li = li0 + k;
-            const uint64_t pg = S / T;
-            if ((li == 0 || S_prev / T != pg) && pg < uint64_t(kMaxTilePages)) {  // first row of its page
+            const uint32_t pg = S / T;
+            if ((li == 0 || pg_prev != pg) && pg < uint32_t(kMaxTilePages)) {  // first row of its page
                 p_row[pg] = uint16_t(li);
                 p_nn[pg]  = uint16_t(NN);
                 p_len[pg] = LEN;
@@ -380,7 +382,7 @@ __global__ void __launch_bounds__(kPackT) k_pack_emit(PackCols P, uint64_t ntile
             if (uint64_t(li) + 1 == t1 - t0) s_np = uint32_t(pg) + 1;
             NN += loc[k] != 0;
             LEN += loc[k] != 0 ? uint32_t(loc_len_field(loc[k])) : 0u;
-            S_prev = S;
+            pg_prev = pg;
             S += c.cost[k];
         }
         __syncthreads();

@@ -261,20 +261,26 @@ __global__ void __launch_bounds__(256)
         uint32_t       s = 0, L = 0, prow = 0;
         int32_t        key = 0;
         uint64_t       pos = 0;
+        bool mixed = false;
         if (have) {
             s    = Ls.l_s[h];
             prow = Ls.l_row[h];
             key  = Ls.l_key[h];
             pos  = off[h];
-            // the bucket end is the next directory word's start; recompute it
+            // a bucket of one key matches whole: its length is the count (the
+            // mixed bitmap, 1 bit per bucket, stays in L2); a mixed bucket's end
+            // is the next directory word's start
             const uint64_t p = bucket_of(fib_hash(key), T.b);
-            L                = uint32_t(__ldg(T.dir + p + 1) >> 16) - s;
+            mixed            = (__ldg(T.mixed + (p >> 5)) >> (p & 31)) & 1u;
+            L                = mixed ? uint32_t(__ldg(T.dir + p + 1) >> 16) - s : Ls.l_cnt[h];
         }
         for (uint32_t k0 = 0; __any_sync(0xffffffffu, have && k0 < L); k0 += G) {
-            const uint32_t k  = s + k0 + gl;
-            const bool     m  = have && k0 + gl < L && __ldg(T.keys + k) == key;
-            const unsigned bl = __ballot_sync(0xffffffffu, m) & gmask;
-            if (m) emit(outs, pos + __popc(bl & ((1u << lane) - 1)), prow, __ldg(T.rows + k));
+            const uint32_t k   = s + k0 + gl;
+            const bool     in  = have && k0 + gl < L;
+            const uint32_t row = in ? __ldg(T.rows + k) : 0u;  // loaded beside the key
+            const bool     m   = in && (!mixed || __ldg(T.keys + k) == key);
+            const unsigned bl  = __ballot_sync(0xffffffffu, m) & gmask;
+            if (m) emit(outs, pos + __popc(bl & ((1u << lane) - 1)), prow, row);
             pos += __popc(bl);
         }
     }
@@ -315,7 +321,20 @@ __global__ void __launch_bounds__(256)
         const uint32_t e0   = min(Ls.b_e[h], s0 + kSplit);
         const uint32_t prow = Ls.b_row[h];
         const uint64_t pos0 = base_pos + big_off[h] + sub * kSplit;
-        for (uint32_t k = s0 + lane; k < e0; k += 32) emit(outs, pos0 + (k - s0), prow, __ldg(T.rows + k));
+        // four loads per lane in flight, then their outputs
+        for (uint32_t k0 = s0; k0 < e0; k0 += 128) {
+            uint32_t r[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const uint32_t k = k0 + 32u * q + lane;
+                r[q]             = k < e0 ? __ldg(T.rows + k) : 0u;
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const uint32_t k = k0 + 32u * q + lane;
+                if (k < e0) emit(outs, pos0 + (k - s0), prow, r[q]);
+            }
+        }
     }
 }
 

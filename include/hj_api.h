@@ -149,7 +149,7 @@ void* hj_context_stream(hj_context* ctx);
  * UnchainedHash::choose_directory_size, capped at 2^dir_cap_bits words),
  * "dir_cap_bits" (default 23: automatic directories of hj_execute stay within
  * 64 MB, cache resident; results do not depend on it), "radix_bits" (partition fan-out of the
- * build, 0..12), "probe_group" (threads per probe key: 1, 4, 8 or 32),
+ * build, 0..12), "probe_group" (threads per probe key in the write pass: 1, 4 (default), 8 or 32),
  * "light_max" (largest bucket scanned by one probe group before the bucket is
  * handed to a whole block), "timing" (1: record per-phase device times of
  * each hj_execute, read with hj_result_phase_ms), "host_access" (1, default:
