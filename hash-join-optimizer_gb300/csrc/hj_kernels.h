@@ -166,6 +166,7 @@ struct VarcharOut {
     uint64_t*       tile_off   = nullptr;  // ntiles + 1 (last = page count, on the device)
     uint64_t        ntiles     = 0;
     PageDesc*       desc       = nullptr;  // varchar_write's page descriptors
+    uint64_t*       recs       = nullptr;  // page starts per tile (packing scratch)
 };
 // All VARCHAR columns of a result at once (their packing kernels share launches).
 void varchar_plan(std::vector<VarcharOut*>& vs, cudaStream_t st);

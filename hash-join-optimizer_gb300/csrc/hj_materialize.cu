@@ -206,6 +206,7 @@ struct PackCol {
     uint32_t*       tile_pages;
     const uint64_t* tile_off;
     PageDesc*       desc;
+    uint64_t*       recs;  // kRec page-start records per tile
 };
 struct PackCols {
     int     n;
@@ -280,18 +281,36 @@ __device__ __forceinline__ void tile_max_any(uint32_t& maxc, bool& any, uint32_t
     __syncthreads();
 }
 
+// Cost of one row from its locator (as row_costs).
+__device__ __forceinline__ uint32_t loc_cost(uint64_t loc) {
+    return loc != 0 ? 8u * (2u + min(uint32_t(loc_len_field(loc)), kPage)) + 1u : 1u;
+}
+
+// Page starts of a prefix-summed tile, kRec records per tile: record p is
+// (first row | non-NULL rows before it << 16 | string bytes before it << 32),
+// tile-relative; record np closes the last page.  Rows cost at most kCap / 8,
+// so a page holds at least 7 rows.  Record 0 of a greedy tile is kGreedyRec.
+constexpr int      kMaxTilePages = kStrTile / 7 + 1;
+constexpr int      kRec          = kMaxTilePages + 1;
+constexpr uint64_t kGreedyRec    = 0xffffull;
+
+__device__ __forceinline__ uint64_t page_rec(uint32_t row, uint32_t nn, uint32_t len) {
+    return uint64_t(row) | (uint64_t(nn) << 16) | (uint64_t(len) << 32);
+}
+
 // Gathers the tile's locators through the row ids into `ol` (read back by the
-// later passes in output order) and counts the tile's pages.
+// later passes in output order), and packs the tile: its page count, and for
+// a prefix-summed tile its page starts.
 __global__ void __launch_bounds__(kPackT) k_pack_count(PackCols P, uint64_t ntiles) {
     __shared__ uint32_t sm[33];
-    __shared__ uint64_t s_sum[kPackT / 32];
-    __shared__ uint32_t s_last;
+    __shared__ uint64_t s_scan[33];
     for (uint64_t g = blockIdx.x; g < ntiles; g += gridDim.x) {
         const PackCol& v  = P.c[pack_col_of(P, g)];
         const uint64_t t  = g - v.tile_base;
         const uint64_t t0 = t * kStrTile, t1 = (v.n < t0 + kStrTile ? v.n : t0 + kStrTile);
         const uint64_t r0 = t0 + uint64_t(threadIdx.x) * kPackRow;
         const uint32_t rows = r0 >= t1 ? 0u : (t1 - r0 < kPackRow ? uint32_t(t1 - r0) : uint32_t(kPackRow));
+        uint64_t*      rec  = v.recs + t * kRec;
         uint64_t       loc[kPackRow];
 #pragma unroll
         for (int k = 0; k < kPackRow; ++k) {
@@ -303,57 +322,15 @@ __global__ void __launch_bounds__(kPackT) k_pack_count(PackCols P, uint64_t ntil
             }
         }
         TileCosts c = row_costs(loc, rows);
-        // cost of the tile without its last row: the start of the last row
-        uint64_t sum = 0;
-#pragma unroll
-        for (int k = 0; k < kPackRow; ++k) {
-            sum += c.cost[k];
-            if (uint32_t(k) + 1 == rows && r0 + rows == t1) s_last = c.cost[k];
-        }
-        sum = warp_sum<uint64_t>(sum);
-        if ((threadIdx.x & 31) == 0) s_sum[threadIdx.x >> 5] = sum;
-        tile_max_any(c.maxc, c.greedy, sm);  // (its barriers also publish s_sum / s_last / ol)
+        tile_max_any(c.maxc, c.greedy, sm);  // (its barriers also publish ol to the block)
         if (c.greedy) {
             if (threadIdx.x < 32) {
                 const uint32_t np = pack_tile(v.ol, v.base, v.npages, t0, t1, nullptr);
-                if (threadIdx.x == 0) v.tile_pages[t] = np;
+                if (threadIdx.x == 0) {
+                    v.tile_pages[t] = np;
+                    rec[0]          = kGreedyRec;
+                }
             }
-        } else if (threadIdx.x == 0) {
-            uint64_t tot = 0;
-            for (int w = 0; w < kPackT / 32; ++w) tot += s_sum[w];
-            v.tile_pages[t] = uint32_t((tot - s_last) / (kCap - c.maxc)) + 1u;
-        }
-        __syncthreads();
-    }
-}
-
-// Cost of one row from its locator (as row_costs).
-__device__ __forceinline__ uint32_t loc_cost(uint64_t loc) {
-    return loc != 0 ? 8u * (2u + min(uint32_t(loc_len_field(loc)), kPage)) + 1u : 1u;
-}
-
-// Page descriptors of each tile, at tile_off[t].
-__global__ void __launch_bounds__(kPackT) k_pack_emit(PackCols P, uint64_t ntiles) {
-    constexpr int kMaxTilePages = kStrTile / 7 + 1;  // rows cost at most kCap / 8: >= 7 rows a page
-    __shared__ uint32_t sm[33];
-    __shared__ uint64_t s_scan[33];
-    __shared__ uint16_t p_row[kMaxTilePages], p_nn[kMaxTilePages];
-    __shared__ uint32_t p_len[kMaxTilePages];
-    __shared__ uint32_t s_np;
-    for (uint64_t g = blockIdx.x; g < ntiles; g += gridDim.x) {
-        const PackCol& v  = P.c[pack_col_of(P, g)];
-        const uint64_t t  = g - v.tile_base;
-        const uint64_t t0 = t * kStrTile, t1 = (v.n < t0 + kStrTile ? v.n : t0 + kStrTile);
-        const uint64_t r0 = t0 + uint64_t(threadIdx.x) * kPackRow;
-        const uint32_t rows = r0 >= t1 ? 0u : (t1 - r0 < kPackRow ? uint32_t(t1 - r0) : uint32_t(kPackRow));
-        uint64_t       loc[kPackRow];
-#pragma unroll
-        for (int k = 0; k < kPackRow; ++k) loc[k] = uint32_t(k) < rows ? v.ol[r0 + k] : 0;
-        TileCosts c = row_costs(loc, rows);
-        tile_max_any(c.maxc, c.greedy, sm);
-        PageDesc* desc = v.desc + v.tile_off[t];
-        if (c.greedy) {
-            if (threadIdx.x < 32) pack_tile(v.ol, v.base, v.npages, t0, t1, desc);
             __syncthreads();
             continue;
         }
@@ -365,36 +342,50 @@ __global__ void __launch_bounds__(kPackT) k_pack_emit(PackCols P, uint64_t ntile
         const uint32_t li0 = uint32_t(r0 - t0);
         uint32_t       NN = uint32_t(pre >> 40), LEN = uint32_t(pre & ((1ull << 40) - 1));
         // S: the row's start in eighths of a byte (offsets, string bytes, one bit per row)
-        uint32_t S = 8u * (2u * NN + LEN) + li0;
-        // start of the row before this thread's first row (the previous thread's last row)
-        uint32_t S_prev = li0 > 0 && rows > 0 ? S - loc_cost(v.ol[r0 - 1]) : 0u;
-        uint32_t pg_prev = S_prev / T;
+        uint32_t S       = 8u * (2u * NN + LEN) + li0;
+        uint32_t pg_prev = li0 > 0 && rows > 0 ? (S - loc_cost(v.ol[r0 - 1])) / T : 0u;
 #pragma unroll
         for (int k = 0; k < kPackRow; ++k) {
             if (uint32_t(k) >= rows) break;
             const uint32_t li = li0 + k;
             const uint32_t pg = S / T;
-            if ((li == 0 || pg_prev != pg) && pg < uint32_t(kMaxTilePages)) {  // first row of its page
-                p_row[pg] = uint16_t(li);
-                p_nn[pg]  = uint16_t(NN);
-                p_len[pg] = LEN;
+            if ((li == 0 || pg_prev != pg) && pg < uint32_t(kMaxTilePages)) rec[pg] = page_rec(li, NN, LEN);
+            if (uint64_t(li) + 1 == t1 - t0) {  // last row: the closing record and the page count
+                const uint32_t np = pg + 1 < uint32_t(kMaxTilePages) ? pg + 1 : uint32_t(kMaxTilePages);
+                rec[np]           = page_rec(uint32_t(t1 - t0), uint32_t(tot >> 40),
+                                             uint32_t(tot & ((1ull << 40) - 1)));
+                v.tile_pages[t]   = np;
             }
-            if (uint64_t(li) + 1 == t1 - t0) s_np = uint32_t(pg) + 1;
             NN += loc[k] != 0;
             LEN += loc[k] != 0 ? uint32_t(loc_len_field(loc[k])) : 0u;
             pg_prev = pg;
             S += c.cost[k];
         }
         __syncthreads();
-        const uint32_t np = s_np < uint32_t(kMaxTilePages) ? s_np : uint32_t(kMaxTilePages);
-        const uint32_t nt = uint32_t(tot >> 40), lt = uint32_t(tot & ((1ull << 40) - 1));
-        for (uint32_t p = threadIdx.x; p < np; p += blockDim.x) {
-            const uint32_t rs = p_row[p], re = p + 1 < np ? p_row[p + 1] : uint32_t(t1 - t0);
-            const uint32_t ns = p_nn[p], ne = p + 1 < np ? p_nn[p + 1] : nt;
-            const uint32_t ls = p_len[p], le = p + 1 < np ? p_len[p + 1] : lt;
-            desc[p] = PageDesc{t0 + rs, re - rs, ne - ns, le - ls, 0};
-        }
-        __syncthreads();
+    }
+}
+
+// Page descriptors at tile_off[t]: one warp per tile, from the page starts of
+// k_pack_count or by the greedy rule.
+__global__ void k_pack_emit(PackCols P, uint64_t ntiles) {
+    const uint64_t g = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    if (g >= ntiles) return;
+    const PackCol&  v    = P.c[pack_col_of(P, g)];
+    const uint64_t  t    = g - v.tile_base;
+    const uint64_t  t0   = t * kStrTile, t1 = (v.n < t0 + kStrTile ? v.n : t0 + kStrTile);
+    const uint64_t* rec  = v.recs + t * kRec;
+    PageDesc*       desc = v.desc + v.tile_off[t];
+    if (rec[0] == kGreedyRec) {
+        pack_tile(v.ol, v.base, v.npages, t0, t1, desc);
+        return;
+    }
+    const uint32_t np = uint32_t(v.tile_off[t + 1] - v.tile_off[t]);
+    for (uint32_t p = threadIdx.x & 31; p < np; p += 32) {
+        const uint64_t a = rec[p], b = rec[p + 1];
+        const uint32_t rs = uint32_t(a & 0xffff), re = uint32_t(b & 0xffff);
+        const uint32_t ns = uint32_t((a >> 16) & 0xffff), ne = uint32_t((b >> 16) & 0xffff);
+        const uint32_t ls = uint32_t(a >> 32), le = uint32_t(b >> 32);
+        desc[p] = PageDesc{t0 + rs, re - rs, ne - ns, le - ls, 0};
     }
 }
 
@@ -559,7 +550,7 @@ void for_pack_groups(std::vector<VarcharOut*>& vs, F&& f) {
         for (size_t i = g0; i < std::min(live.size(), g0 + kMaxPackCols); ++i) {
             VarcharOut& v = *live[i];
             P.c[P.n++]    = PackCol{v.locs, v.rid, v.ol, v.base, v.base_pages, v.n, v.ntiles, tiles,
-                                 v.tile_pages, v.tile_off, v.desc};
+                                 v.tile_pages, v.tile_off, v.desc, v.recs};
             tiles += v.ntiles;
         }
         f(P, tiles);
@@ -575,6 +566,7 @@ void varchar_plan(std::vector<VarcharOut*>& vs, cudaStream_t st) {
         v.ntiles     = (v.n + kStrTile - 1) / kStrTile;
         v.tile_pages = dalloc_n<uint32_t>(v.ntiles, st);
         v.tile_off   = dalloc_n<uint64_t>(v.ntiles + 1, st);
+        v.recs       = dalloc_n<uint64_t>(v.ntiles * kRec, st);
     }
     for_pack_groups(vs, [&](const PackCols& P, uint64_t tiles) {
         k_pack_count<<<grid_of(tiles, 4), kPackT, 0, st>>>(P, tiles);
@@ -590,7 +582,7 @@ std::vector<uint8_t*> varchar_write(std::vector<VarcharOut*>& vs, const std::vec
     for (size_t i = 0; i < vs.size(); ++i)
         if (vs[i]->n) vs[i]->desc = static_cast<PageDesc*>(dalloc(std::max<uint64_t>(pages[i], 1) * sizeof(PageDesc), st));
     for_pack_groups(vs, [&](const PackCols& P, uint64_t tiles) {
-        k_pack_emit<<<grid_of(tiles, 4), kPackT, 0, st>>>(P, tiles);
+        k_pack_emit<<<div_up(tiles * 32, 256), 256, 0, st>>>(P, tiles);
         HJ_LAUNCH_CHECK();
     });
     for (size_t i = 0; i < vs.size(); ++i) {
@@ -602,11 +594,13 @@ std::vector<uint8_t*> varchar_write(std::vector<VarcharOut*>& vs, const std::vec
         k_write_varchar_pages<<<grid_of(div_up(pages[i], kVW), 3), kVW * 32, kVW * kPage, st>>>(
             v.desc, pages[i], v.ol, v.base, v.base_pages, out[i]);
         HJ_LAUNCH_CHECK();
-        for (void* p : {(void*)v.desc, (void*)v.ol, (void*)v.tile_pages, (void*)v.tile_off}) dfree(p, st);
+        for (void* p : {(void*)v.desc, (void*)v.ol, (void*)v.tile_pages, (void*)v.tile_off, (void*)v.recs})
+            dfree(p, st);
         v.desc       = nullptr;
         v.ol         = nullptr;
         v.tile_pages = nullptr;
         v.tile_off   = nullptr;
+        v.recs       = nullptr;
     }
     return out;
 }
