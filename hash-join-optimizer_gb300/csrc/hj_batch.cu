@@ -235,22 +235,33 @@ __global__ void __launch_bounds__(kPT)
     }
 }
 
-// 3. rows into partition order.  Shared memory: the item's rows sorted by
-// partition (keys, payloads), then per partition its count, its first sorted
-// row and its global base.
-__global__ void __launch_bounds__(kPT)
+// 4-byte global -> shared copy that completes asynchronously (cp.async);
+// cp_async_wait_all waits for this thread's copies.
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+    const uint32_t sa = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// 3. rows into partition order.  Shared memory: the item's payloads in row
+// order (copied asynchronously while the keys are ranked), its keys sorted by
+// partition with each one's row in the item, then per partition its count,
+// its first sorted row and its global base.
+__global__ void __launch_bounds__(kPT, 2)
     k_bpart_scatter(const RelInst* __restrict__ R, uint32_t nr, uint64_t items, unsigned long long* q,
                     const uint64_t* __restrict__ off, uint32_t* __restrict__ fill, uint32_t pmax,
                     int32_t* __restrict__ okey, int32_t* __restrict__ opay) {
     extern __shared__ __align__(16) unsigned char smem[];
-    int32_t*  skey  = reinterpret_cast<int32_t*>(smem);
-    int32_t*  spay  = skey + kPartItem;
-    uint32_t* hist  = reinterpret_cast<uint32_t*>(spay + kPartItem);
+    int32_t*  spay  = reinterpret_cast<int32_t*>(smem);   // row order
+    int32_t*  skey  = spay + kPartItem;                    // partition order
+    uint32_t* hist  = reinterpret_cast<uint32_t*>(skey + kPartItem);
     uint32_t* loff  = hist + (1u << pmax);
     uint64_t* gbase = reinterpret_cast<uint64_t*>(loff + (1u << pmax));
+    uint16_t* sidx  = reinterpret_cast<uint16_t*>(gbase + (1u << pmax));  // partition order: row in the item
     __shared__ unsigned long long sh;
     __shared__ uint32_t           wsum[32];
     constexpr int kPer = kPartItem / kPT;
+    static_assert(kPartItem <= 65536, "row in the item fits 16 bits");
     for (uint64_t t = next_item(q, &sh); t < items; t = next_item(q, &sh)) {
         const RelInst& s  = R[owner(nr, t, [&](uint32_t i) { return R[i].item_base; })];
         const uint64_t r0 = (t - s.item_base) * kPartItem;
@@ -259,6 +270,11 @@ __global__ void __launch_bounds__(kPT)
         const uint32_t pb  = s.pbits;
         const uint32_t np2 = 1u << pb;
         for (uint32_t k = threadIdx.x; k < np2; k += kPT) hist[k] = 0;
+#pragma unroll
+        for (int j = 0; j < kPer; ++j) {
+            const uint32_t i = threadIdx.x + uint32_t(j) * kPT;
+            if (r0 + i < r1) cp_async4(spay + i, s.pay + r0 + i);
+        }
         __syncthreads();
         uint32_t pr[kPer];  // partition << 16 | rank in the partition
         int32_t  kv[kPer];
@@ -284,13 +300,14 @@ __global__ void __launch_bounds__(kPT)
         smem_scan(loff, np2, false, wsum);
 #pragma unroll
         for (int j = 0; j < kPer; ++j) {
-            const uint64_t r = r0 + threadIdx.x + uint64_t(j) * kPT;
-            if (r < r1) {
+            const uint32_t i = threadIdx.x + uint32_t(j) * kPT;
+            if (r0 + i < r1) {
                 const uint32_t pos = loff[pr[j] >> 16] + (pr[j] & 0xffffu);
                 skey[pos]          = kv[j];
-                spay[pos]          = __ldg(s.pay + r);
+                sidx[pos]          = uint16_t(i);
             }
         }
+        cp_async_wait_all();
         __syncthreads();
         const uint32_t m = uint32_t(r1 - r0);
         for (uint32_t j = threadIdx.x; j < m; j += kPT) {
@@ -298,8 +315,9 @@ __global__ void __launch_bounds__(kPT)
             const uint32_t p   = part_of(k, pb);
             const uint64_t pos = gbase[p] + (j - loff[p]);
             okey[pos]          = k;
-            opay[pos]          = spay[j];
+            opay[pos]          = spay[sidx[j]];
         }
+        __syncthreads();  // the next item overwrites spay
     }
 }
 
@@ -427,8 +445,15 @@ __global__ void __launch_bounds__(kPT, 2)
         const int32_t* pk = key + x0;
         const int32_t* pp = pay + x0;
         unsigned long long my_rows = 0, my_sum = 0;
+        // the next row's key and payload are loaded while this row is looked up
+        int32_t k_next = threadIdx.x < m ? __ldg(pk + threadIdx.x) : 0;
+        int32_t p_next = threadIdx.x < m ? __ldg(pp + threadIdx.x) : 0;
         for (uint32_t x = threadIdx.x; x < m; x += kPT) {
-            const int32_t k = __ldg(pk + x);
+            const int32_t k = k_next, pv = p_next;
+            if (x + kPT < m) {
+                k_next = __ldg(pk + x + kPT);
+                p_next = __ldg(pp + x + kPT);
+            }
             uint32_t      cj[kMaxRel];  // matches << 16 | first match (tables hold < 2^16 rows)
             bool          all = true, dup = false;
 #pragma unroll
@@ -450,7 +475,7 @@ __global__ void __launch_bounds__(kPT, 2)
                 }
             }
             if (!all) continue;
-            uint64_t fp = fp_start(k, __ldg(pp + x));
+            uint64_t fp = fp_start(k, pv);
             if (!dup) {
 #pragma unroll
                 for (uint32_t j = 0; j < kMaxRel; ++j) {
@@ -645,7 +670,7 @@ std::vector<uint32_t> batch_execute(const std::vector<BatchInstance>& B, const B
 
     // persistent grids (occupancy queries are not capturable: take them first)
     const size_t hist_smem = (size_t(1) << pmax) * 4;
-    const size_t scat_smem = size_t(kPartItem) * 8 + (size_t(1) << pmax) * 16;
+    const size_t scat_smem = size_t(kPartItem) * 10 + (size_t(1) << pmax) * 16;
     const int    g_hist    = resident_grid(k_bpart_hist, hist_smem);
     const int    g_scat    = resident_grid(k_bpart_scatter, scat_smem);
     const int    g_join    = resident_grid(k_bjoin, join_smem);
