@@ -205,10 +205,21 @@ __device__ __forceinline__ void smem_scan(uint32_t* a, uint32_t n, bool inclusiv
 __global__ void __launch_bounds__(kPT)
     k_bpart_hist(const RelInst* __restrict__ R, uint32_t nr, uint64_t items, unsigned long long* q,
                  uint32_t* __restrict__ cnt) {
+    // The block's counts accumulate in shared memory over the consecutive items
+    // it takes from one relation and go to global memory when the relation
+    // changes (items are numbered relation by relation), not once per item.
     extern __shared__ uint32_t hist[];
     __shared__ unsigned long long sh;
+    uint32_t cur = ~0u;  // relation whose counts the shared histogram holds
+    auto flush = [&]() {
+        if (cur == ~0u) return;
+        const RelInst& c = R[cur];
+        for (uint32_t k = threadIdx.x; k < (1u << c.pbits); k += kPT)
+            if (hist[k]) atomicAdd(cnt + c.part_base + k, hist[k]);
+    };
     for (uint64_t t = next_item(q, &sh); t < items; t = next_item(q, &sh)) {
-        const RelInst& s  = R[owner(nr, t, [&](uint32_t i) { return R[i].item_base; })];
+        const uint32_t ri = owner(nr, t, [&](uint32_t i) { return R[i].item_base; });
+        const RelInst& s  = R[ri];
         const uint64_t r0 = (t - s.item_base) * kPartItem;
         const uint64_t r1 = min(s.rows, r0 + kPartItem);
         if (r0 >= r1) continue;
@@ -217,8 +228,13 @@ __global__ void __launch_bounds__(kPT)
             continue;
         }
         const uint32_t np2 = 1u << s.pbits;
-        for (uint32_t k = threadIdx.x; k < np2; k += kPT) hist[k] = 0;
-        __syncthreads();
+        if (ri != cur) {  // (next_item's barriers order these against the last item's atomics)
+            flush();
+            __syncthreads();
+            for (uint32_t k = threadIdx.x; k < np2; k += kPT) hist[k] = 0;
+            cur = ri;
+            __syncthreads();
+        }
         constexpr int kPer = kPartItem / kPT;
         int32_t       kv[kPer];
 #pragma unroll
@@ -229,10 +245,9 @@ __global__ void __launch_bounds__(kPT)
 #pragma unroll
         for (int j = 0; j < kPer; ++j)
             if (r0 + threadIdx.x + uint64_t(j) * kPT < r1) atomicAdd(&hist[part_of(kv[j], s.pbits)], 1u);
-        __syncthreads();
-        for (uint32_t k = threadIdx.x; k < np2; k += kPT)
-            if (hist[k]) atomicAdd(cnt + s.part_base + k, hist[k]);
     }
+    __syncthreads();
+    flush();
 }
 
 // 4-byte global -> shared copy that completes asynchronously (cp.async);
@@ -424,18 +439,43 @@ __global__ void __launch_bounds__(kPT, 2)
         // build the tables
         for (uint32_t w = threadIdx.x; w < words; w += kPT) S[w] = 0;
         __syncthreads();
-        for (uint32_t j = 0; j < nt; ++j)
-            for (uint32_t r = threadIdx.x; r < g_tn[j]; r += kPT)
-                atomicAdd(&S[g_ts[j] + bucket(j, __ldg(key + g_src[j] + r)) + 1], 1u);
+        // four rows per thread in flight per step, loads before the atomics
+        constexpr uint32_t kBU = 4;
+        for (uint32_t j = 0; j < nt; ++j) {
+            const uint32_t tn = g_tn[j];
+            const int32_t* kj = key + g_src[j];
+            for (uint32_t r = threadIdx.x; r < tn; r += kBU * kPT) {
+                int32_t kk[kBU];
+#pragma unroll
+                for (uint32_t u = 0; u < kBU; ++u) kk[u] = r + u * kPT < tn ? __ldg(kj + r + u * kPT) : 0;
+#pragma unroll
+                for (uint32_t u = 0; u < kBU; ++u)
+                    if (r + u * kPT < tn) atomicAdd(&S[g_ts[j] + bucket(j, kk[u]) + 1], 1u);
+            }
+        }
         __syncthreads();
         smem_scan(S, words, true, wsum);
-        for (uint32_t j = 0; j < nt; ++j)
-            for (uint32_t r = threadIdx.x; r < g_tn[j]; r += kPT) {
-                const int32_t  k   = __ldg(key + g_src[j] + r);
-                const uint32_t pos = atomicSub(&S[g_ts[j] + bucket(j, k) + 1], 1u) - 1;
-                skey[pos]          = k;
-                spay[pos]          = __ldg(pay + g_src[j] + r);
+        for (uint32_t j = 0; j < nt; ++j) {
+            const uint32_t tn = g_tn[j];
+            const int32_t* kj = key + g_src[j];
+            const int32_t* pj = pay + g_src[j];
+            for (uint32_t r = threadIdx.x; r < tn; r += kBU * kPT) {
+                int32_t kk[kBU], pv[kBU];
+#pragma unroll
+                for (uint32_t u = 0; u < kBU; ++u) {
+                    const bool in = r + u * kPT < tn;
+                    kk[u]         = in ? __ldg(kj + r + u * kPT) : 0;
+                    pv[u]         = in ? __ldg(pj + r + u * kPT) : 0;
+                }
+#pragma unroll
+                for (uint32_t u = 0; u < kBU; ++u)
+                    if (r + u * kPT < tn) {
+                        const uint32_t pos = atomicSub(&S[g_ts[j] + bucket(j, kk[u]) + 1], 1u) - 1;
+                        skey[pos]          = kk[u];
+                        spay[pos]          = pv[u];
+                    }
             }
+        }
         __syncthreads();
         // probe the item's R0 rows
         const uint64_t p0 = off[s.part_base + l];
