@@ -336,10 +336,11 @@ __global__ void __launch_bounds__(kPT, 2)
     }
 }
 
-// R0 rows of one join work item: at least 8 per build row, so the table build
-// is amortised.
+// R0 rows of one join work item: at least 16 per build row, so the table build
+// is amortised (a partition of a probe side 10x its build side is then one
+// item, its tables built once).
 __device__ __forceinline__ uint64_t join_chunk(uint64_t build_rows) {
-    const uint64_t c = 8 * build_rows;
+    const uint64_t c = 16 * build_rows;
     return c > kJoinChunk ? c : uint64_t(kJoinChunk);
 }
 
