@@ -205,11 +205,12 @@ __device__ __forceinline__ void smem_scan(uint32_t* a, uint32_t n, bool inclusiv
 __global__ void __launch_bounds__(kPT)
     k_bpart_hist(const RelInst* __restrict__ R, uint32_t nr, uint64_t items, unsigned long long* q,
                  uint32_t* __restrict__ cnt) {
-    // The block's counts accumulate in shared memory over the consecutive items
-    // it takes from one relation and go to global memory when the relation
-    // changes (items are numbered relation by relation), not once per item.
+    // Items of equal size go to the blocks round robin (no queue, no barrier
+    // per item).  The block's counts accumulate in shared memory over its items
+    // of one relation and go to global memory when the relation changes (items
+    // are numbered relation by relation), not once per item.
     extern __shared__ uint32_t hist[];
-    __shared__ unsigned long long sh;
+    (void)q;
     uint32_t cur = ~0u;  // relation whose counts the shared histogram holds
     auto flush = [&]() {
         if (cur == ~0u) return;
@@ -217,7 +218,7 @@ __global__ void __launch_bounds__(kPT)
         for (uint32_t k = threadIdx.x; k < (1u << c.pbits); k += kPT)
             if (hist[k]) atomicAdd(cnt + c.part_base + k, hist[k]);
     };
-    for (uint64_t t = next_item(q, &sh); t < items; t = next_item(q, &sh)) {
+    for (uint64_t t = blockIdx.x; t < items; t += gridDim.x) {
         const uint32_t ri = owner(nr, t, [&](uint32_t i) { return R[i].item_base; });
         const RelInst& s  = R[ri];
         const uint64_t r0 = (t - s.item_base) * kPartItem;
@@ -228,7 +229,8 @@ __global__ void __launch_bounds__(kPT)
             continue;
         }
         const uint32_t np2 = 1u << s.pbits;
-        if (ri != cur) {  // (next_item's barriers order these against the last item's atomics)
+        if (ri != cur) {
+            __syncthreads();  // the last item's atomics are done
             flush();
             __syncthreads();
             for (uint32_t k = threadIdx.x; k < np2; k += kPT) hist[k] = 0;
