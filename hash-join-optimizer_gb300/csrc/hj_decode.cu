@@ -106,7 +106,7 @@ __global__ void __launch_bounds__(kDecThreads)
     }
 }
 
-__global__ void __launch_bounds__(kDecThreads)
+__global__ void __launch_bounds__(kDecThreads, 8)
     k_decode_varchar_loc(const uint8_t* __restrict__ pages, uint64_t num_pages,
                          const uint64_t* __restrict__ row_start, uint64_t* __restrict__ out) {
     for (uint64_t p = global_warp(); p < num_pages; p += total_warps()) {
