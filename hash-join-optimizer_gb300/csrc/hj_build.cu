@@ -245,7 +245,15 @@ __global__ void __launch_bounds__(kThreads)
             const uint64_t h     = fib_hash(tkey[j]);
             const uint32_t local = uint32_t(bucket_of(h, g.b)) & lmask;
             bucket_add(cnt, local, act);
-            atomicOr(blm + local, bloom_mask(h));
+            // a warp of one heavy key ORs its tags once, not 32 times on one word
+            uint32_t   first = 0;
+            const bool uni   = __match_all_sync(act, local, reinterpret_cast<int*>(&first)) != 0;
+            if (uni) {
+                const uint32_t all = __reduce_or_sync(act, bloom_mask(h));
+                if (int(threadIdx.x & 31) == __ffs(act) - 1) atomicOr(blm + local, all);
+            } else {
+                atomicOr(blm + local, bloom_mask(h));
+            }
         }
     }
     __syncthreads();
@@ -453,11 +461,23 @@ __global__ void __launch_bounds__(kThreads)
     bool     single;
     if (!chunk_range(blockIdx.x, chunk_off, part_off, 1u << g.R, part, s, e, single)) return;
     if (fused_part(part_off, part)) return;  // set by k_bucket_local
-    for (uint32_t j = s + threadIdx.x; j < e; j += blockDim.x) {
-        const int32_t  k     = key[j];
-        const uint64_t p     = bucket_of(fib_hash(k), g.b);
-        const uint64_t first = __ldg(dir + p) >> 16;
-        if (key[first] != k) atomicOr(mixed + (p >> 5), 1u << (p & 31));
+    // four tuples per thread at a time: keys, then directory words, then first keys
+    for (uint32_t j0 = s + threadIdx.x; j0 < e; j0 += 4 * blockDim.x) {
+        int32_t  k[4];
+        uint64_t p[4], first[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const uint32_t j = j0 + u * blockDim.x;
+            k[u]             = j < e ? key[j] : 0;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            p[u]     = bucket_of(fib_hash(k[u]), g.b);
+            first[u] = j0 + u * blockDim.x < e ? __ldg(dir + p[u]) >> 16 : 0;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (j0 + u * blockDim.x < e && key[first[u]] != k[u]) atomicOr(mixed + (p[u] >> 5), 1u << (p[u] & 31));
     }
 }
 
