@@ -61,7 +61,7 @@ def parse():
     ap.add_argument("--opt", action="append", default=[], metavar="NAME=VALUE",
                     help="engine option for the timed runs (hj_set_option), repeatable")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--e2e-depth", type=int, default=2,
+    ap.add_argument("--e2e-depth", type=int, default=3,
                     help="plans in flight in the pipelined end-to-end mode (1 = serial only)")
     ap.add_argument("--e2e-pageable", action="store_true",
                     help="end to end from pageable host memory (GPU gather / scatter) instead of page-locked")
