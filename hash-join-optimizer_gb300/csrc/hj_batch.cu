@@ -103,11 +103,13 @@ __global__ void k_batch_generate(uint64_t seed, uint32_t inst, uint32_t rel, uin
 // rows per partition summed over its build relations); a row belongs to
 // partition top_p_i(hash(key)).
 //   1. row counts per (relation, partition), all relations of all instances
-//                                                            k_bpart_hist
+//      (8192-row items round robin; counts kept per block until its
+//      relation changes)                                     k_bpart_hist
 //   2. exclusive scan -> partition offsets in one partitioned buffer
 //   3. rows into partition order                             k_bpart_scatter
-//      (block-local counting sort in shared memory, one global range
-//      reservation per (block, partition), runs written out coalesced)
+//      (block-local counting sort in shared memory, payloads staged by
+//      cp.async meanwhile, one global range reservation per (block,
+//      partition), runs written out coalesced)
 //   4. join work list: (instance partition, chunk of its R0 rows)
 //                                                            k_bjoin_plan
 //   5. per work item: the partition of every build relation becomes a
@@ -117,7 +119,7 @@ __global__ void k_batch_generate(uint64_t seed, uint32_t inst, uint32_t rel, uin
 // duplicates) flags its instance, which is then recomputed on the plain path.
 constexpr int      kPT         = 512;   // threads of the partition and join blocks
 constexpr uint32_t kPartItem   = 8192;  // rows per partition-pass work item
-constexpr uint32_t kJoinChunk  = 8192;  // least R0 rows per join work item
+constexpr uint32_t kJoinChunk  = 8192;  // least R0 rows per join work item (else 16 per build row)
 constexpr uint32_t kMaxPartBits = 11;
 constexpr uint32_t kMaxRel     = 8;     // relations per instance
 
@@ -203,14 +205,12 @@ __device__ __forceinline__ void smem_scan(uint32_t* a, uint32_t n, bool inclusiv
 
 // 1. per (relation, partition) row counts
 __global__ void __launch_bounds__(kPT)
-    k_bpart_hist(const RelInst* __restrict__ R, uint32_t nr, uint64_t items, unsigned long long* q,
-                 uint32_t* __restrict__ cnt) {
+    k_bpart_hist(const RelInst* __restrict__ R, uint32_t nr, uint64_t items, uint32_t* __restrict__ cnt) {
     // Items of equal size go to the blocks round robin (no queue, no barrier
     // per item).  The block's counts accumulate in shared memory over its items
     // of one relation and go to global memory when the relation changes (items
     // are numbered relation by relation), not once per item.
     extern __shared__ uint32_t hist[];
-    (void)q;
     uint32_t cur = ~0u;  // relation whose counts the shared histogram holds
     auto flush = [&]() {
         if (cur == ~0u) return;
@@ -727,7 +727,7 @@ std::vector<uint32_t> batch_execute(const std::vector<BatchInstance>& B, const B
         HJ_CUDA(cudaMemsetAsync(cnt, 0, (pbase + 1) * 4, st));
         HJ_CUDA(cudaMemsetAsync(fill, 0, (pbase + 1) * 4, st));
         if (items) {
-            k_bpart_hist<<<grid_for(g_hist, items), kPT, hist_smem, st>>>(d_R, nr, items, d_q + 0, cnt);
+            k_bpart_hist<<<grid_for(g_hist, items), kPT, hist_smem, st>>>(d_R, nr, items, cnt);
             HJ_LAUNCH_CHECK();
         }
         scan_exclusive_u32_to_u64_into(cnt, off, pbase, tmp, st);
