@@ -110,7 +110,8 @@ __global__ void __launch_bounds__(1024)
 //    partition's space, the items are placed partition by partition in shared
 //    memory and then stored so that consecutive threads write consecutive
 //    slots of a partition (runs instead of single 4-byte stores).
-__global__ void __launch_bounds__(kThreads, 2)
+template <int kST>  // threads; a tile is kST * kItems rows
+__global__ void __launch_bounds__(kST, 1024 / kST)
     k_part_scatter(KeyCol kc, uint32_t R, uint32_t* __restrict__ part_cursor,
                    int32_t* __restrict__ tkey, uint32_t* __restrict__ trow) {
     extern __shared__ uint32_t sh[];  // P counters / tile offsets, P global bases, staged items
@@ -119,9 +120,10 @@ __global__ void __launch_bounds__(kThreads, 2)
     uint32_t*      off   = sh;                   // counts, then the tile's partition offsets
     uint32_t*      gbase = sh + P;               // global slot of each partition's first item
     int32_t*       sk    = reinterpret_cast<int32_t*>(sh + 2 * P);
-    uint32_t*      sr    = sh + 2 * P + kTile;
-    uint16_t*      sp    = reinterpret_cast<uint16_t*>(sh + 2 * P + 2 * kTile);  // partition of each slot
-    const uint64_t tile0 = uint64_t(blockIdx.x) * kTile;
+    constexpr int  kT    = kST * kItems;
+    uint32_t*      sr    = sh + 2 * P + kT;
+    uint16_t*      sp    = reinterpret_cast<uint16_t*>(sh + 2 * P + 2 * kT);  // partition of each slot
+    const uint64_t tile0 = uint64_t(blockIdx.x) * kT;
     for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) off[i] = 0;
     __syncthreads();
     int32_t  keys[kItems];
@@ -129,7 +131,7 @@ __global__ void __launch_bounds__(kThreads, 2)
     uint32_t okmask = 0;
 #pragma unroll
     for (int k = 0; k < kItems; ++k) {
-        const uint64_t i  = tile0 + uint64_t(k) * kThreads + threadIdx.x;
+        const uint64_t i  = tile0 + uint64_t(k) * kST + threadIdx.x;
         const bool     ok = load_key(kc, i, keys[k]);
         parts[k]          = ok ? uint32_t(bucket_of(fib_hash(keys[k]), R)) : 0;
         rank[k]           = ok ? atomicAdd(off + parts[k], 1u) : 0;
@@ -137,7 +139,7 @@ __global__ void __launch_bounds__(kThreads, 2)
     }
     __syncthreads();
     // exclusive scan of the counts (thread t: partitions [t * per, (t + 1) * per))
-    const uint32_t per = (P + kThreads - 1) / kThreads;
+    const uint32_t per = (P + kST - 1) / kST;
     uint32_t       run = 0;
     for (uint32_t q = 0; q < per; ++q) {
         const uint32_t p = threadIdx.x * per + q;
@@ -164,7 +166,7 @@ __global__ void __launch_bounds__(kThreads, 2)
         if ((okmask >> k) & 1u) {
             const uint32_t q = off[parts[k]] + rank[k];
             sk[q]            = keys[k];
-            sr[q]            = uint32_t(tile0 + uint64_t(k) * kThreads + threadIdx.x);
+            sr[q]            = uint32_t(tile0 + uint64_t(k) * kST + threadIdx.x);
             sp[q]            = uint16_t(parts[k]);
         }
     }
@@ -515,7 +517,8 @@ void build_table(const KeyCol& kc, int dir_bits, int radix_bits, Table& t, uint6
     if (R > kMaxRadix) throw Error(HJ_ERR_INVALID, "build side too large for the radix partition");
 
     prefer_shared(k_part_hist);
-    prefer_shared(k_part_scatter);
+    prefer_shared(k_part_scatter<1024>);
+    prefer_shared(k_part_scatter<kThreads>);
     prefer_shared(k_bucket_count);
     prefer_shared(k_bucket_scatter);
     prefer_shared(k_bucket_local);
@@ -564,9 +567,19 @@ void build_table(const KeyCol& kc, int dir_bits, int radix_bits, Table& t, uint6
     int32_t*  tkey = dalloc_n<int32_t>(nv, st);
     uint32_t* trow = dalloc_n<uint32_t>(nv, st);
     {
-        const size_t smem = (2 * size_t(P) + 2 * size_t(kTile)) * sizeof(uint32_t) + kTile * sizeof(uint16_t);
-        HJ_CUDA(cudaFuncSetAttribute(k_part_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-        k_part_scatter<<<div_up(kc.n, kTile), kThreads, smem, st>>>(kc, R, part_cursor, tkey, trow);
+        // 16384-row tiles (runs of about 8 items per partition at 2048
+        // partitions) when the shared memory allows, else 8192-row tiles
+        auto smem_for = [&](size_t tile) { return (2 * size_t(P) + 2 * tile) * sizeof(uint32_t) + tile * sizeof(uint16_t); };
+        const size_t big = smem_for(size_t(1024) * kItems);
+        if (big <= 200 * 1024) {
+            HJ_CUDA(cudaFuncSetAttribute(k_part_scatter<1024>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(big)));
+            k_part_scatter<1024><<<div_up(kc.n, 1024 * kItems), 1024, big, st>>>(kc, R, part_cursor, tkey, trow);
+        } else {
+            const size_t smem = smem_for(kTile);
+            HJ_CUDA(cudaFuncSetAttribute(k_part_scatter<kThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         int(smem)));
+            k_part_scatter<kThreads><<<div_up(kc.n, kTile), kThreads, smem, st>>>(kc, R, part_cursor, tkey, trow);
+        }
         HJ_LAUNCH_CHECK();
     }
 
