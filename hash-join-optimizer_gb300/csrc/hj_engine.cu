@@ -903,18 +903,26 @@ struct Exec {
             varchar_plan(vptr, c->st);
         }
         std::vector<uint64_t> vpages;
-        if (!vout.empty()) {  // one synchronisation for the page counts of every VARCHAR column
+        cudaEvent_t           counted = nullptr;
+        if (!vout.empty()) {  // one readback for the page counts of every VARCHAR column
             phase("mat_sync");
             for (size_t i = 0; i < vout.size(); ++i)
                 readback(c->pinned + i, vout[i].second.tile_off + vout[i].second.ntiles, sizeof(uint64_t), true,
                          c->st);  // page-locked scratch
-            HJ_CUDA(cudaStreamSynchronize(c->st));
-            vpages.assign(c->pinned, c->pinned + vout.size());
+            HJ_CUDA(cudaEventCreateWithFlags(&counted, cudaEventDisableTiming));
+            HJ_CUDA(cudaEventRecord(counted, c->st));
         }
-        // the INT32 pages keep the GPU busy while the host sizes the VARCHAR buffers
+        // the INT32 pages keep the GPU busy while the host waits for the page
+        // counts and sizes the VARCHAR buffers
         phase("materialize");
         for (const IntOut& o : iout)
             launch_write_int32_pages(o.col, o.rid, o.rows, res->cols[o.a].pages->as<uint8_t>(), c->st);
+        if (counted) {
+            const cudaError_t e = cudaEventSynchronize(counted);
+            cudaEventDestroy(counted);
+            HJ_CUDA(e);
+            vpages.assign(c->pinned, c->pinned + vout.size());
+        }
         if (!vout.empty()) {
             phase("mat_varchar_write");
             const std::vector<uint8_t*> bufs = varchar_write(vptr, vpages, c->st);
