@@ -194,3 +194,22 @@ def test_read_plans_json(hj, tmp_path):
     parsed = fe.parse_sql(SQL)
     plan, _ = fe.load_join_pipeline(plans["x1"], parsed, SCHEMA, fe.table_loader(hj, data(), SCHEMA), hj)
     assert len(plan.nodes) == 5
+
+
+def test_parse_sql_forms(hj):
+    """Aliases without AS, nested groups, NOT IN over strings, comments, no WHERE."""
+    from hjgb300 import frontend as fe
+    p = fe.parse_sql("""SELECT a.x, MIN(b.y) -- comment
+                        FROM t a, u b
+                        WHERE a.k = b.k AND ((a.s NOT IN ('p', 'q''s') AND a.x <> 3) OR a.x IS NULL)""")
+    assert p.tables == {"a": "t", "b": "u"}
+    assert p.aggregates == [("", "a", "x"), ("MIN", "b", "y")]
+    f = p.filters["a"]
+    assert f.kind == "or" and f.args[0].kind == "and"
+    assert f.args[0].args[0].kind == "not" and f.args[0].args[0].args[0].value == ["p", "q's"]
+    q = fe.parse_sql("SELECT a.x FROM t AS a;")
+    assert q.filters == {} and q.join_graph == {"a": {}}
+    with pytest.raises(fe.FrontEndError):
+        fe.parse_sql("SELECT a.x FROM t AS a, t AS a")
+    with pytest.raises(fe.FrontEndError):
+        fe.parse_sql("SELECT z.x FROM t AS a")

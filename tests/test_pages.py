@@ -73,3 +73,42 @@ def test_empty_and_all_null_columns(hj, orc):
     col = hj.Column.varchar([None] * 100 + [""] * 3)
     b, o, m = orc.decode_column(3, col.pages)
     assert m.tolist() == [0] * 100 + [1] * 3
+
+
+def test_prefix_sum_packing_rule_fits_and_stays_near_greedy():
+    """The VARCHAR page rule of the GPU writer (k_pack_count): a row costs
+    8 * (2 + len) + 1 eighths of a byte (NULL: 1), a page holds sum <= cap =
+    65497 eighths, and row i of a 4096-row tile goes to page floor(S_i / T)
+    with S_i the exclusive prefix and T = cap - (largest cost in the tile).
+    Checked here on random tiles: every page fits, none is empty, and the page
+    count is at most cap / T times the greedy rule's (the reference's) plus one:
+    within 1% for strings of up to 64 bytes."""
+    cap = 65536 - 32 - 7
+    rng = np.random.default_rng(12)
+    for trial in range(40):
+        n = int(rng.integers(1, 4097))
+        hi = [16, 64, 300, 1000][trial % 4]
+        lens = rng.integers(0, hi + 1, n)
+        null = rng.random(n) < 0.1
+        cost = np.where(null, 1, 8 * (2 + lens) + 1).astype(np.int64)
+        T = cap - int(cost.max())
+        S = np.concatenate([[0], np.cumsum(cost)[:-1]])
+        page = S // T
+        npages = int(page[-1]) + 1
+        assert np.array_equal(np.unique(page), np.arange(npages))  # no empty page
+        for p in range(npages):
+            c = cost[page == p]
+            nn = int((~null[page == p]).sum())
+            nbytes = int(lens[(page == p) & ~null].sum())
+            rows = int(c.size)
+            assert 4 + 2 * nn + nbytes + (rows + 7) // 8 <= 8192
+        greedy, cur = 1, 0  # greedy: append while the page still fits
+        for c in cost:
+            if cur + c > cap:
+                greedy, cur = greedy + 1, 0
+            cur += c
+        # pages are at least T / cap full: at most cap / T times greedy's count,
+        # which is within 1% for strings of up to 64 bytes
+        assert npages <= greedy * cap / T + 1
+        if hi <= 64:
+            assert npages <= greedy * 1.01 + 1
