@@ -14,11 +14,14 @@ build, probe, and the output written as reference-format pages.
          the copy of every result page back to host memory in the timed region
   roofline  the probe phase (count + write kernels) against measured HBM
          bandwidth, algorithmic bytes 4*N_probe + 8*D + 8*N_build + 8*N_out
-  cpu_baseline  the oracle restatement of the reference's execute() on a
-         bounded prefix of the probe side, all host threads
+  cpu_baseline  the oracle restatement of the reference's execute() on the
+         same inputs, all host threads (the whole workload when it takes at
+         most about 30 s of CPU time, else a stated probe-side prefix)
 
 The inputs (>2 GB of pages) exceed the 126 MB L2, so no flush is needed
-between steps.  `--impl reference` times the CPU restatement alone.
+between steps.  `--impl reference` times the CPU restatement alone, one
+execute() of the same workload per step, with input pages built by the
+oracle's own page writers (the engine library is never loaded).
 Multi-GPU (torchrun): independent replicas, one per GPU (the path has no
 exchange step); value = all ranks' probe tuples / max step time.
 """
@@ -41,7 +44,7 @@ sys.path.insert(0, str(ROOT))
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=["c1", "c2", "c2raw", "c3", "c4", "c5"], default="c2")
@@ -55,8 +58,12 @@ def parse():
     ap.add_argument("--plain-instances", type=int, default=-1,
                     help="c4: instances timed on the plain path (-1 = all)")
     ap.add_argument("--scale", type=float, default=1.0)
-    ap.add_argument("--cpu-sample", type=int, default=2_000_000,
-                    help="probe rows of the bounded CPU-baseline sample")
+    ap.add_argument("--cpu-budget-s", type=float, default=30.0,
+                    help="CPU seconds the cpu_baseline leg may spend; a prefix of the probe side is timed "
+                         "when one execute() of the whole workload would exceed it")
+    ap.add_argument("--ref-budget-s", type=float, default=240.0,
+                    help="--impl reference: seconds for all steps; a probe-side prefix per step when the "
+                         "whole workload would exceed it")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--opt", action="append", default=[], metavar="NAME=VALUE",
                     help="engine option for the timed runs (hj_set_option), repeatable")
@@ -178,17 +185,53 @@ def ncu_traffic(workload: str):
     return None
 
 
-def cpu_port_run(plan):
-    """Times one execute() of the oracle restatement; returns (seconds, rows)."""
+def oracle_mod():
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle
-    lib = oracle.port()
-    t = time.perf_counter()
-    out = oracle.run(lib, plan)
-    dt = time.perf_counter() - t
-    if out.status != 0:
-        raise RuntimeError(out.error)
-    return dt, out.num_rows
+    return oracle
+
+
+def workload_config(w, args, world: int, build_tuples: int, probe_tuples: int, output_rows: int) -> dict:
+    """The `config` of a plain-path line; both arms print the same one."""
+    raw = w.meta.get("probe_rows_raw")
+    desc = {"c1": "c1: 1,000,000 build x 10,000,000 probe rows, unique permuted keys",
+            "c2": f"c2: {w.build_rows} build x {raw} raw probe rows ({w.probe_rows} after the pre-filter)",
+            "c2raw": f"c2raw: {w.build_rows} build x {raw} raw probe rows, predicate pred < 100 in the plan",
+            "c3": "c3: 5-relation left-deep chain, " + " / ".join(str(k) for k in w.meta.get("kept", []))
+                  + " rows after the pre-filters (of " + " / ".join(str(k) for k in w.meta.get("sizes", [])) + ")"}
+    return {"workload": desc.get(w.name, w.name), "scale": args.scale, "build_tuples": build_tuples,
+            "probe_tuples": probe_tuples, "output_rows": output_rows, "parallelism": f"replicas x{world}",
+            "l2": "inputs larger than L2"}
+
+
+def cpu_reference_steps(w, oracle, steps: int, warmup: int, budget_s: float):
+    """Times `steps` restated execute() calls after `warmup` untimed ones, all
+    host threads.  The whole workload per call when (steps + warmup) calls fit
+    in budget_s (judged from the first call), else the plan's probe-side
+    prefix sized to fit.  Returns (seconds per step, probe tuples per step,
+    stats of the last call, sample description)."""
+    threads = os.cpu_count() or 1
+    os.environ["SIGMOD_THREADS"] = str(threads)
+    first = oracle.timed_execute(w.plan)
+    plan, k = w.plan, None
+    per_call = first["seconds"]
+    if (steps + max(0, warmup - 1)) * per_call > budget_s and w.sample is not None:
+        frac = budget_s / ((steps + warmup) * per_call)
+        k = max(1, int(w.probe_rows * frac))
+        plan = w.sample(k)
+    for _ in range(max(0, warmup - 1)):
+        oracle.timed_execute(plan)
+    times, st = [], first
+    for _ in range(steps):
+        st = oracle.timed_execute(plan)
+        times.append(st["seconds"])
+    if k is None:
+        sample = (f"the whole workload per step ({st['build_tuples']} build and {st['probe_tuples']} probe tuples, "
+                  f"{st['rows']} result rows); execute() to finished result pages, {threads} threads")
+    else:
+        sample = (f"first {k} of {w.probe_rows} probe rows against the whole build side per step (the whole "
+                  f"workload took {per_call:.1f} s per execute()); {threads} threads")
+    return statistics.median(times), st["probe_tuples"], st, sample
 
 
 # --------------------------------------------------------- end to end ---
@@ -202,8 +245,9 @@ def run_e2e(args, d: Dist, hj, eng, w, npr: int, out_pages: list, stream) -> dic
     pipelined: the same steps through hj_server with --e2e-depth plans in
                flight, so that the upload of one plan, the kernels of another
                and the result download of a third overlap (the link carries
-               both directions at once for page-locked memory).  `value` is
-               this mode when --e2e-depth > 1."""
+               both directions at once for page-locked memory).
+    Both modes are reported (`modes`); `value` is the faster one, named in
+    `mode`."""
     import ctypes as C
     import collections
     import numpy as np
@@ -251,7 +295,7 @@ def run_e2e(args, d: Dist, hj, eng, w, npr: int, out_pages: list, stream) -> dic
         parts["fetch_ms"] += 1e3 * (time.perf_counter() - t1)
         eng.free_result(r)
 
-    def timed(fn, k, blocks=3):
+    def timed(fn, k, blocks=5):
         """Median over `blocks` timed blocks of k steps: the host link is shared
         with the machine's other GPUs, whose traffic shows up as outlier blocks."""
         per = []
@@ -273,11 +317,12 @@ def run_e2e(args, d: Dist, hj, eng, w, npr: int, out_pages: list, stream) -> dic
             parts[key] = 0.0
         d2h_seen.clear()
         serial_ms, serial_blocks = timed(lambda k: [serial_step() for _ in range(k)], k2)
+        modes = {"serial": {"ms_per_step": serial_ms, "blocks_ms_per_step": [round(x, 3) for x in serial_blocks],
+                            "parts_ms": {key: round(v / (len(serial_blocks) * k2), 3) for key, v in parts.items()}}}
         out = {"value": npr * d.world / (serial_ms / 1e3), "unit": "probe tuples/s", "ms_per_step": serial_ms,
                "mode": "serial", "host_memory": "pageable" if args.e2e_pageable else "page-locked",
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": int(sum(d2h_seen) / max(1, len(d2h_seen))),
-               "parts_ms": {key: round(v / (3 * k2), 3) for key, v in parts.items()},
-               "blocks_ms_per_step": [round(x, 3) for x in serial_blocks]}
+               "modes": modes}
         depth = args.e2e_depth
         if depth > 1:
             srv = hj.Server(eng, hbm_budget_bytes=int(args.budget_gb * 2**30), slots=depth)
@@ -294,15 +339,18 @@ def run_e2e(args, d: Dist, hj, eng, w, npr: int, out_pages: list, stream) -> dic
                         r, _st = srv.wait(q.popleft())
                         fetch(r)
                         eng.free_result(r)
-                pipelined(3 * depth)  # warm the slots (first plans of a slot set up its pools)
                 kp = max(k2, 3 * depth)
+                # warm the slots: each slot's first plans set up its stream's pools
+                for _ in range(2):
+                    pipelined(kp)
                 pipe_ms, pipe_blocks = timed(pipelined, kp)
             finally:
                 srv.close()
-            out.update({"value": npr * d.world / (pipe_ms / 1e3), "ms_per_step": pipe_ms,
-                        "mode": f"pipelined through hj_server, {depth} plans in flight",
-                        "blocks_ms_per_step": [round(x, 3) for x in pipe_blocks],
-                        "serial_ms_per_step": serial_ms})
+            modes["pipelined"] = {"ms_per_step": pipe_ms, "plans_in_flight": depth,
+                                  "blocks_ms_per_step": [round(x, 3) for x in pipe_blocks]}
+            if pipe_ms < serial_ms:
+                out.update({"value": npr * d.world / (pipe_ms / 1e3), "ms_per_step": pipe_ms,
+                            "mode": f"pipelined through hj_server, {depth} plans in flight"})
         return out
     finally:
         for a in locked:
@@ -356,25 +404,32 @@ def run_ours(args, d: Dist) -> dict:
             for k, v in ph.items():
                 phase_sum[k] = phase_sum.get(k, 0.0) + v
             launches += int(ph["launches"])
-            eng.free_result(r)
+            last = r
+            if _ < args.steps - 1:
+                eng.free_result(r)
         end.record(stream)
         torch.cuda.synchronize()
         d.barrier()
+    last_counters = eng.counters(last)
+    eng.free_result(last)
     ms = d.max(start.elapsed_time(end) / args.steps)
     clocks = clk.summary()
     phases = {k: round(v / args.steps, 4) for k, v in phase_sum.items() if k != "launches"}
 
-    # ---- roofline of the probe phase
-    dir_bits = max(0, int(np.ceil(np.log2(max(1, nb)))))
-    D = (1 << dir_bits) + 1
-    a_probe = 4 * npr + 8 * D + 8 * nb + 8 * nout
+    # ---- roofline of the probe phase: directory words and table tuples of
+    # the tables this execute built (summed over its joins)
+    cnt = last_counters
+    D, nt = cnt["dir_words"], cnt["table_tuples"]
+    a_probe = 4 * npr + 8 * D + 8 * nt + 8 * nout
     # the probe kernels: count + write, without the host readback between them
     t_probe = (phases.get("probe", 0.0) + phases.get("probe_write", 0.0)) / 1e3
     peak, peak_kind = peaks()
     achieved = a_probe / t_probe / 1e9 if t_probe > 0 else None
-    roofline = {"bound": "hbm", "kernel": "probe (k_probe_count + k_write_*)", "achieved": achieved,
+    roofline = {"bound": "hbm", "kernel": "probe (count + write kernels)", "achieved": achieved,
                 "peak": peak, "unit": "GB/s", "frac": achieved / peak if achieved else None,
                 "traffic": ncu_traffic(args.workload), "algorithmic_bytes": a_probe,
+                "bytes_formula": f"4*N_probe + 8*D + 8*N_table + 8*N_out = 4*{npr} + 8*{D} + 8*{nt} + 8*{nout}",
+                "probe_ms": t_probe * 1e3,
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind}
 
     # ---- end to end through the C ABI with host buffers
@@ -382,29 +437,23 @@ def run_ours(args, d: Dist) -> dict:
     if not args.no_e2e:
         e2e = run_e2e(args, d, hj, eng, w, npr, out_pages, stream)
 
-    # ---- CPU baseline (rank 0, bounded sample)
+    # ---- CPU baseline (rank 0): the oracle restatement on the same inputs
     cpu = None
-    if d.rank == 0 and not args.no_cpu_baseline and w.sample is not None:
-        k = min(args.cpu_sample, w.probe_rows)
-        os.environ.setdefault("SIGMOD_THREADS", str(os.cpu_count() or 1))
-        dt, _ = cpu_port_run(w.sample(k))
-        cpu = {"value": k / dt, "unit": "probe tuples/s", "cores": int(os.environ["SIGMOD_THREADS"]),
-               "kind": "port",
-               "sample": f"first {k} of {w.probe_rows} probe rows against the full {w.build_rows}-row build "
-                         f"side, one execute() incl. build and output pages ({dt:.2f} s)"}
+    if d.rank == 0 and not args.no_cpu_baseline:
+        sec, ptup, _st, sample = cpu_reference_steps(w, oracle_mod(), 1, 1, args.cpu_budget_s)
+        cpu = {"value": ptup / sec, "unit": "probe tuples/s", "cores": os.cpu_count() or 1, "kind": "port",
+               "sample": sample + f"; {sec:.2f} s per execute()"}
 
     for t in resident.inputs:
         eng.release(t)
     eng.close()
     return {
-        "metric": "probe tuples/s", "value": npr * d.world / (ms / 1e3), "unit": "tuples/s",
+        "metric": "probe tuples/s", "value": npr * d.world / (ms / 1e3), "unit": "probe tuples/s",
         "n_gpus": d.world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
         "data": "synthetic (seeded generator with the configured shapes; inputs > L2, no flush needed)",
-        "config": {"workload": f"{w.name}: {w.build_rows} build x {w.meta.get('probe_rows_raw', w.probe_rows)} "
-                               f"raw probe rows ({w.probe_rows} after the pre-filter)",
-                   "scale": args.scale, "build_tuples": nb, "probe_tuples": npr, "output_rows": nout,
-                   "parallelism": f"replicas x{d.world}", "l2": "inputs larger than L2"},
+        "config": workload_config(w, args, d.world, nb, npr, nout),
+        "build_tuples_per_s": nb * d.world / (ms / 1e3),
         "phases_ms": phases, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
         "gpu_launches": launches, "clocks": clocks,
     }
@@ -528,28 +577,33 @@ def run_serve(args, d: Dist) -> dict:
 
 
 def run_reference(args, d: Dist):
+    """The reference's CPU path (the oracle restatement of Contest::execute,
+    all host threads) on the same workload and config as the GPU arm: one
+    execute() per step, input pages built by the oracle's own writers, so the
+    engine library is never loaded.  Rank 0 alone runs under torchrun."""
     if d.rank != 0:
         return None
+    if args.workload in ("c4", "c5"):
+        return {"impl": "reference", "unavailable": f"{args.workload} is compared against the plain GPU path; "
+                                                      "the CPU reference arm covers c1, c2, c2raw and c3"}
+    oracle = oracle_mod()
     from __graft_entry__ import load
-    hj = load()
+    hj = load()  # Plan / Table types only; the page writers below are the oracle's
+    hj.use_page_writer(oracle.page_writer)
     w = make_workload(hj, args.workload, args.scale)
-    k = min(args.cpu_sample, w.probe_rows)
-    plan = w.sample(k) if w.sample else w.plan
+    if w.name == "c2raw":  # the oracle takes pre-filtered tables, as the reference's execute() does
+        w.plan = w.meta["prefiltered_plan"]
+    sec, ptup, st, sample = cpu_reference_steps(w, oracle, args.steps, args.warmup, args.ref_budget_s)
+    v = ptup / sec
     threads = os.cpu_count() or 1
-    os.environ["SIGMOD_THREADS"] = str(threads)
-    for _ in range(args.warmup):
-        cpu_port_run(plan)
-    times = [cpu_port_run(plan)[0] for _ in range(args.steps)]
-    ms = 1e3 * sum(times) / len(times)
-    v = k / (ms / 1e3)
-    sample = (f"first {k} of {w.probe_rows} probe rows against the full {w.build_rows}-row build side; "
-              f"one execute() per step incl. build and output pages")
-    return {"impl": "reference", "metric": "probe tuples/s", "value": v, "unit": "tuples/s", "n_gpus": d.world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-            "config": {"workload": w.name, "scale": args.scale, "probe_tuples": k},
-            "cpu_baseline": {"value": v, "unit": "tuples/s", "cores": threads, "kind": "port", "sample": sample},
-            "e2e": {"value": v, "unit": "tuples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    return {"impl": "reference", "metric": "probe tuples/s", "value": v, "unit": "probe tuples/s",
+            "n_gpus": d.world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic (seeded generator with the configured shapes)",
+            "config": workload_config(w, args, d.world, st["build_tuples"], st["probe_tuples"], st["rows"]),
+            "cpu_baseline": {"value": v, "unit": "probe tuples/s", "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": v, "unit": "probe tuples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
 def main():

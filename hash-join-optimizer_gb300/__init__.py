@@ -32,7 +32,7 @@ EXPORTS = [
     "hj_context_create", "hj_context_destroy", "hj_last_error", "hj_version", "hj_context_stream",
     "hj_set_option", "hj_get_option", "hj_table_upload", "hj_table_release",
     "hj_execute", "hj_result_shape", "hj_result_column", "hj_result_copy_pages",
-    "hj_result_copy_contiguous", "hj_result_stats", "hj_result_phase_ms", "hj_result_free",
+    "hj_result_copy_contiguous", "hj_result_stats", "hj_result_phase_ms", "hj_result_counter", "hj_result_free",
     "hj_table_build", "hj_table_info", "hj_table_probe", "hj_table_free",
     "hj_pages_from_int32", "hj_pages_from_strings", "hj_table_probe_noalloc",
     "hj_batch_execute", "hj_batch_generate", "hj_table_prepare",
@@ -133,6 +133,7 @@ def lib() -> C.CDLL:
     L.hj_host_register.argtypes = [vp, u64]
     L.hj_host_unregister.argtypes = [vp]
     L.hj_result_stats.argtypes = [vp, P(u64), P(u64), P(u64)]
+    L.hj_result_counter.argtypes = [vp, C.c_char_p, P(u64)]
     L.hj_result_free.argtypes = [vp]
     L.hj_table_build.argtypes = [vp, vp, vp, u64, i32, P(vp)]
     L.hj_table_info.argtypes = [vp, P(u32), P(u64), P(vp), P(vp), P(vp)]
@@ -164,6 +165,21 @@ def _ptr(a: Optional[np.ndarray]) -> Optional[int]:
     return None if a is None else a.ctypes.data
 
 
+# Writer of host pages for Column.int32 / Column.varchar: None = the library's
+# hj_pages_from_int32 / hj_pages_from_strings.
+_page_writer = None
+
+
+def use_page_writer(fn) -> None:
+    """Builds host tables with `fn(kind, *arrays) -> (n, 8192) uint8 pages`
+    (kind "int32": (values, valid); "strings": (bytes, offsets, valid)) instead
+    of the library's writers, so that a process that only prepares
+    reference-format tables need not load the GPU library.  None restores the
+    library's writers."""
+    global _page_writer
+    _page_writer = fn
+
+
 # --------------------------------------------------------------- host tables --
 
 @dataclass
@@ -181,6 +197,8 @@ class Column:
         """Packs like Table::to_columnar (src/build_table.cpp:666-700)."""
         v = np.ascontiguousarray(values, dtype=np.int32)
         m = None if valid is None else np.ascontiguousarray(valid, dtype=np.uint8)
+        if _page_writer is not None:
+            return Column(INT32, _page_writer("int32", v, m))
         n = C.c_uint64()
         L = lib()
         _check(None, L.hj_pages_from_int32(_ptr(v), _ptr(m), v.size, None, 0, C.byref(n)))
@@ -202,6 +220,8 @@ class Column:
         o = np.ascontiguousarray(offsets, dtype=np.uint64)
         m = None if valid is None else np.ascontiguousarray(valid, dtype=np.uint8)
         nrows = o.size - 1
+        if _page_writer is not None:
+            return Column(VARCHAR, _page_writer("strings", b, o, m))
         n = C.c_uint64()
         L = lib()
         bp = _ptr(b) if b.size else None
@@ -438,6 +458,15 @@ class Engine:
             L.hj_result_phase_ms(res, name.encode(), C.byref(ms))
             ph[name] = ms.value
         return b.value, p.value, o.value, ph
+
+    def counters(self, res: int) -> dict:
+        """hj_result_counter: directory words, table tuples, joins and kernel launches of a result."""
+        out = {}
+        for name in ("dir_words", "table_tuples", "joins", "launches"):
+            v = C.c_uint64()
+            _check(self._ctx, lib().hj_result_counter(res, name.encode(), C.byref(v)))
+            out[name] = v.value
+        return out
 
     def free_result(self, res: int) -> None:
         lib().hj_result_free(res)

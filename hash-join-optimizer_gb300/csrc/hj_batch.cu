@@ -609,7 +609,7 @@ int resident_grid(K kernel, size_t smem) {
     int per_sm = 0;
     HJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kPT, smem));
     if (per_sm < 1) throw Error(HJ_ERR_INVALID, "batch: a kernel does not fit on an SM");
-    return per_sm * kSMs;
+    return per_sm * num_sms();
 }
 
 }  // namespace
@@ -623,7 +623,7 @@ void launch_batch_generate(uint64_t seed, uint32_t instance, uint32_t relation, 
     if (match_q24 > (1u << 24)) throw Error(HJ_ERR_INVALID, "batch_generate: match rate above 2^24");
     if (rows == 0) return;
     if (!keys || !payload) throw Error(HJ_ERR_INVALID, "batch_generate: null output");
-    const unsigned blocks = unsigned(std::min<uint64_t>(div_up(rows, 256), uint64_t(kSMs) * 16));
+    const unsigned blocks = unsigned(std::min<uint64_t>(div_up(rows, 256), uint64_t(num_sms()) * 16));
     k_batch_generate<<<blocks, 256, 0, st>>>(seed, instance, relation, build_rows, match_q24, rows, keys, payload);
     HJ_LAUNCH_CHECK();
 }
@@ -736,7 +736,7 @@ std::vector<uint32_t> batch_execute(const std::vector<BatchInstance>& B, const B
                                                                              pkey, ppay);
             HJ_LAUNCH_CHECK();
         }
-        k_bjoin_plan<<<unsigned(std::min<uint64_t>(div_up(ipbase, 256), uint64_t(kSMs) * 8)), 256, 0, st>>>(
+        k_bjoin_plan<<<unsigned(std::min<uint64_t>(div_up(ipbase, 256), uint64_t(num_sms()) * 8)), 256, 0, st>>>(
             d_I, n, ipbase, off, jcnt);
         HJ_LAUNCH_CHECK();
         scan_exclusive_u32_to_u64_into(jcnt, joff, ipbase, tmp, st);
@@ -837,7 +837,7 @@ void plain_instance(const BatchInstance& b, const ProbeParams& prm, int dir_bits
         int32_t*  nk = last ? nullptr : static_cast<int32_t*>(take(total * 4));
         uint64_t* nf = last ? nullptr : static_cast<uint64_t*>(take(total * 8));
         if (total) {
-            k_pairs_next<<<unsigned(std::min<uint64_t>(div_up(total, 256), uint64_t(kSMs) * 8)), 256, 0, st>>>(
+            k_pairs_next<<<unsigned(std::min<uint64_t>(div_up(total, 256), uint64_t(num_sms()) * 8)), 256, 0, st>>>(
                 pr, bw, total, pkeys, pfp, ppay, br.payload, nk, nf, d_sum);
             HJ_LAUNCH_CHECK();
         }

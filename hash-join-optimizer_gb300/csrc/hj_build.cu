@@ -497,7 +497,7 @@ uint32_t ceil_log2(uint64_t n) {
 
 int grid_for(uint64_t work, int threads, int per_sm = 4) {
     const uint64_t want = (work + threads - 1) / threads;
-    return int(std::min<uint64_t>(std::max<uint64_t>(want, 1), uint64_t(kSMs) * per_sm));
+    return int(std::min<uint64_t>(std::max<uint64_t>(want, 1), uint64_t(num_sms()) * per_sm));
 }
 
 }  // namespace
@@ -610,7 +610,7 @@ void build_table(const KeyCol& kc, int dir_bits, int radix_bits, Table& t, uint6
         const size_t nl   = size_t(1) << g.L;
         const size_t smem = (nl + (nl + 1) / 2 + (nl + 31) / 32 + 2 * size_t(kFuseMax)) * sizeof(uint32_t);
         HJ_CUDA(cudaFuncSetAttribute(k_bucket_local, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-        k_bucket_local<<<std::min<uint32_t>(P, uint32_t(kSMs)), kLT, smem, st>>>(g, part_off, tkey, trow, t.dir,
+        k_bucket_local<<<std::min<uint32_t>(P, uint32_t(num_sms())), kLT, smem, st>>>(g, part_off, tkey, trow, t.dir,
                                                                                 t.keys, t.rows, t.mixed);
         HJ_LAUNCH_CHECK();
     }

@@ -15,7 +15,11 @@ namespace hj {
 constexpr int      kPage       = 8192;
 constexpr int      kDenseRows  = 1984;        // rows of a full INT32 page (no NULLs)
 constexpr uint64_t kFib        = 11400714819323198485ull;  // 2^64 / golden ratio
-constexpr int      kSMs        = 152;         // GB300: 2 dies x 76 SMs
+
+// Multiprocessors of the current device (152 on a GB300: 2 dies x 76), read
+// once per device from cudaDevAttrMultiProcessorCount; grids are sized in
+// multiples of it.
+int num_sms();
 
 // Engine error carrying an HJ_* status; converted to a return code at the C ABI.
 struct Error : std::runtime_error {

@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(kDecThreads, 8)
 // one warp per page: kDecThreads / 32 pages per block
 unsigned page_grid(uint64_t num_pages) {
     const uint64_t blocks = (num_pages + kDecThreads / 32 - 1) / (kDecThreads / 32);
-    return unsigned(std::max<uint64_t>(1, std::min<uint64_t>(blocks, uint64_t(kSMs) * 8)));
+    return unsigned(std::max<uint64_t>(1, std::min<uint64_t>(blocks, uint64_t(num_sms()) * 8)));
 }
 
 }  // namespace

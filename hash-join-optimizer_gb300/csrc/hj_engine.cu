@@ -40,6 +40,22 @@ namespace hj {
 
 std::atomic<uint64_t> g_kernel_launches{0};
 
+int num_sms() {
+    constexpr int           kMaxDev = 64;
+    static std::atomic<int> cache[kMaxDev];
+    int                     dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) dev = 0;
+    const int slot = dev < kMaxDev ? dev : kMaxDev - 1;
+    int       n    = cache[slot].load(std::memory_order_relaxed);
+    if (n > 0) return n;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) {
+        cudaGetLastError();  // leave no sticky status behind
+        n = 152;
+    }
+    if (dev < kMaxDev) cache[slot].store(n, std::memory_order_relaxed);
+    return n;
+}
+
 // ---------------------------------------------------------------- memory ----
 
 // Large blocks (result pages, decoded columns, row-id streams: >= 64 MB) are
@@ -362,6 +378,7 @@ struct hj_result {
     };
     std::vector<Col> cols;
     uint64_t         build_tuples = 0, probe_tuples = 0, output_rows = 0;
+    uint64_t         dir_words = 0, table_tuples = 0, joins = 0;  // summed over the joins
     uint64_t         kernel_launches = 0;     // kernels this execute launched
     std::map<std::string, double> phase_ms;  // filled when option "timing" is 1
 };
@@ -597,6 +614,7 @@ struct Exec {
     const hj_plan_desc&                    plan;
     std::vector<std::shared_ptr<DevTable>> tables;
     uint64_t                               build_tuples = 0, probe_tuples = 0, out_rows = 0;
+    uint64_t                               dir_words = 0, table_tuples = 0, joins = 0;
     std::vector<std::pair<std::string, cudaEvent_t>> marks;  // phase boundaries (timing)
 
     // Starts phase `name` on the stream (no-op unless option "timing" is set).
@@ -800,6 +818,9 @@ struct Exec {
             build_table(bkc, int(c->dir_bits), int(c->radix_bits), t, c->pinned, c->st, hint,
                         int(c->dir_cap_bits));
         }
+        ++joins;
+        table_tuples += t.n_tuples;
+        if (t.n_tuples) dir_words += (uint64_t(1) << t.dir_bits) + 1;
         phase("probe");
         ProbeParams prm;
         prm.light_max = int(c->light_max);
@@ -1251,6 +1272,9 @@ int hj_execute(hj_context* c, const hj_plan_desc* plan, hj_result** out) {
         res->build_tuples = ex.build_tuples;
         res->probe_tuples = ex.probe_tuples;
         res->output_rows  = ex.out_rows;
+        res->dir_words    = ex.dir_words;
+        res->table_tuples = ex.table_tuples;
+        res->joins        = ex.joins;
     });
     res->kernel_launches = hj::g_kernel_launches.load() - launches0;
     if (rc != HJ_OK) {
@@ -1349,6 +1373,17 @@ int hj_result_phase_ms(const hj_result* r, const char* phase, double* ms) {
     }
     auto it = r->phase_ms.find(phase);
     *ms     = it == r->phase_ms.end() ? 0.0 : it->second;
+    return HJ_OK;
+}
+
+int hj_result_counter(const hj_result* r, const char* name, uint64_t* value) {
+    if (!r || !name || !value) return HJ_ERR_INVALID;
+    const std::string n(name);
+    if (n == "dir_words") *value = r->dir_words;
+    else if (n == "table_tuples") *value = r->table_tuples;
+    else if (n == "joins") *value = r->joins;
+    else if (n == "launches") *value = r->kernel_launches;
+    else return HJ_ERR_INVALID;
     return HJ_OK;
 }
 

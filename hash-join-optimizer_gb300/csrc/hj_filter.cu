@@ -155,7 +155,7 @@ uint64_t filter_compact(const Filters& f, uint64_t n, uint32_t* rid_out, uint64_
     if (n > 0xffffffffull) throw Error(HJ_ERR_INVALID, "a filtered scan has more than 2^32 rows");
     const uint64_t ntiles = (n + kFTile - 1) / kFTile;
     const uint64_t nwords = (n + 31) / 32;
-    const unsigned grid   = unsigned(std::min<uint64_t>(ntiles, uint64_t(kSMs) * 8));
+    const unsigned grid   = unsigned(std::min<uint64_t>(ntiles, uint64_t(num_sms()) * 8));
     uint32_t*      words  = dalloc_n<uint32_t>(nwords, st);
     uint32_t*      cnt    = dalloc_n<uint32_t>(ntiles, st);
     uint64_t*      off    = dalloc_n<uint64_t>(ntiles + 1, st);

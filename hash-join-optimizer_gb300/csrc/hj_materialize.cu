@@ -524,7 +524,7 @@ __global__ void __launch_bounds__(kVW * 32)
 }
 
 unsigned grid_of(uint64_t items, uint64_t per_sm = 16) {
-    return unsigned(std::max<uint64_t>(1, std::min<uint64_t>(items, uint64_t(kSMs) * per_sm)));
+    return unsigned(std::max<uint64_t>(1, std::min<uint64_t>(items, uint64_t(num_sms()) * per_sm)));
 }
 
 }  // namespace

@@ -14,7 +14,10 @@
 // looked up once per device (with that device current) through
 // cudaGetSymbolAddress and passed to the kernels.  That lookup happens in the
 // first call on each device, so that first call should come before any
-// stream capture.  All calls share the array and it keeps the last call's
+// stream capture.  The address belongs to the device's primary context (the
+// runtime's); it is kept until the process exits, so neither a non-primary
+// driver-API context nor a call after cudaDeviceReset is supported.  All
+// calls share the array and it keeps the last call's
 // contents; the counters that must start at zero are cleared on every call.
 // Two calls whose GPU work overlaps (different streams, or different contexts
 // on one device) race on the array and must be serialised by the caller.

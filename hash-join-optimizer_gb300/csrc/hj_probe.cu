@@ -215,7 +215,7 @@ __global__ void __launch_bounds__(kPT)
 // Grid of the count pass: up to 8 blocks of 256 threads per SM, looping over
 // the tiles (measured faster than a register-capped single resident wave).
 int probe_count_grid(uint64_t ntiles) {
-    return int(std::max<uint64_t>(1, std::min<uint64_t>(ntiles, uint64_t(kSMs) * 8)));
+    return int(std::max<uint64_t>(1, std::min<uint64_t>(ntiles, uint64_t(num_sms()) * 8)));
 }
 
 __global__ void __launch_bounds__(512) k_mixed_count(ProbeTab T, Lists Ls) {
@@ -426,7 +426,7 @@ uint64_t probe_count(const Table& t, const KeyCol& pk, const ProbeParams& prm, P
     const int      grid   = probe_count_grid(ntiles);
     k_probe_count<<<grid, kPT, 0, st>>>(T, pk, prm.light_max, L, ntiles);
     HJ_LAUNCH_CHECK();
-    k_mixed_count<<<kSMs * 2, 512, 0, st>>>(T, L);
+    k_mixed_count<<<num_sms() * 2, 512, 0, st>>>(T, L);
     HJ_LAUNCH_CHECK();
     if (prm.after_count) prm.after_count();
     pp->host = prm.pinned;
@@ -454,7 +454,7 @@ void probe_write(const Table& t, const KeyCol& pk, ProbePlan* pp, const RidOut* 
     if (pp->n_light) {
         uint64_t* off = dalloc_n<uint64_t>(pp->n_light + 1, st);
         scan_exclusive_u32_to_u64(L.l_cnt, off, pp->n_light, st);
-        const int grid = int(std::min<uint64_t>(div_up(pp->n_light, 256), uint64_t(kSMs) * 16));
+        const int grid = int(std::min<uint64_t>(div_up(pp->n_light, 256), uint64_t(num_sms()) * 16));
         switch (pp->group) {
         case 1: k_write_light<1><<<grid, 256, 0, st>>>(T, L, pp->n_light, off, outs); break;
         case 4: k_write_light<4><<<grid, 256, 0, st>>>(T, L, pp->n_light, off, outs); break;
@@ -478,16 +478,16 @@ void probe_write(const Table& t, const KeyCol& pk, ProbePlan* pp, const RidOut* 
         uint32_t*      unit_hit  = dalloc_n<uint32_t>(max_units, st);
         k_unit_map<<<div_up(pp->n_big, 256), 256, 0, st>>>(unit_off, pp->n_big, unit_hit);
         HJ_LAUNCH_CHECK();
-        k_write_big<<<kSMs * 8, 256, 0, st>>>(T, L, pp->n_big, unit_off, unit_hit, big_off, pp->tot_light, outs);
+        k_write_big<<<num_sms() * 8, 256, 0, st>>>(T, L, pp->n_big, unit_off, unit_hit, big_off, pp->tot_light, outs);
         HJ_LAUNCH_CHECK();
         for (void* p : {(void*)units, (void*)lens, (void*)unit_off, (void*)big_off, (void*)unit_hit}) dfree(p, st);
     }
     if (pp->n_mixed) {
         uint64_t* off = dalloc_n<uint64_t>(pp->n_mixed + 1, st);
         scan_exclusive_u32_to_u64(L.m_cnt, off, pp->n_mixed, st);
-        k_write_mixed_warp<<<kSMs * 8, 256, 0, st>>>(T, L, off, pp->tot_light + pp->tot_big, outs);
+        k_write_mixed_warp<<<num_sms() * 8, 256, 0, st>>>(T, L, off, pp->tot_light + pp->tot_big, outs);
         HJ_LAUNCH_CHECK();
-        k_write_mixed<<<kSMs * 2, 512, 0, st>>>(T, L, off, pp->tot_light + pp->tot_big, outs);
+        k_write_mixed<<<num_sms() * 2, 512, 0, st>>>(T, L, off, pp->tot_light + pp->tot_big, outs);
         HJ_LAUNCH_CHECK();
         dfree(off, st);
     }
@@ -553,7 +553,7 @@ int probe_into_scratch(const Table& t, const KeyCol& pk, const ProbeParams& prm,
     const int      grid   = probe_count_grid(ntiles);
     k_probe_count<<<grid, kPT, 0, st>>>(T, pk, prm.light_max, L, ntiles);
     HJ_LAUNCH_CHECK();
-    k_mixed_count<<<kSMs * 2, 512, 0, st>>>(T, L);
+    k_mixed_count<<<num_sms() * 2, 512, 0, st>>>(T, L);
     HJ_LAUNCH_CHECK();
     uint64_t* h = prm.pinned;
     readback(h, L.ctr, 6 * sizeof(uint64_t), true, st);  // page-locked scratch
@@ -569,7 +569,7 @@ int probe_into_scratch(const Table& t, const KeyCol& pk, const ProbeParams& prm,
     outs.o[1] = RidOut{1, nullptr, out_build};
     if (n_light) {
         scan_exclusive_u32_to_u64_into(L.l_cnt, light_off, n_light, tmp, st);
-        const int g = int(std::min<uint64_t>(div_up(n_light, 256), uint64_t(kSMs) * 16));
+        const int g = int(std::min<uint64_t>(div_up(n_light, 256), uint64_t(num_sms()) * 16));
         switch (prm.group) {
         case 1: k_write_light<1><<<g, 256, 0, st>>>(T, L, n_light, light_off, outs); break;
         case 4: k_write_light<4><<<g, 256, 0, st>>>(T, L, n_light, light_off, outs); break;
@@ -592,14 +592,14 @@ int probe_into_scratch(const Table& t, const KeyCol& pk, const ProbeParams& prm,
             k_unit_map<<<div_up(n_big, 256), 256, 0, st>>>(unit_off, n_big, unit_hit);
             HJ_LAUNCH_CHECK();
         }
-        k_write_big<<<kSMs * 8, 256, 0, st>>>(T, L, n_big, unit_off, unit_hit, big_off, tot_light, outs);
+        k_write_big<<<num_sms() * 8, 256, 0, st>>>(T, L, n_big, unit_off, unit_hit, big_off, tot_light, outs);
         HJ_LAUNCH_CHECK();
     }
     if (n_mixed) {
         scan_exclusive_u32_to_u64_into(L.m_cnt, mixed_off, n_mixed, tmp, st);
-        k_write_mixed_warp<<<kSMs * 8, 256, 0, st>>>(T, L, mixed_off, tot_light + tot_big, outs);
+        k_write_mixed_warp<<<num_sms() * 8, 256, 0, st>>>(T, L, mixed_off, tot_light + tot_big, outs);
         HJ_LAUNCH_CHECK();
-        k_write_mixed<<<kSMs * 2, 512, 0, st>>>(T, L, mixed_off, tot_light + tot_big, outs);
+        k_write_mixed<<<num_sms() * 2, 512, 0, st>>>(T, L, mixed_off, tot_light + tot_big, outs);
         HJ_LAUNCH_CHECK();
     }
     return HJ_OK;

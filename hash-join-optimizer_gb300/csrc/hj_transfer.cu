@@ -97,7 +97,7 @@ bool page_locked(const void* p) {
 
 unsigned warp_grid(uint64_t pages) {
     const uint64_t blocks = (pages + kTT / 32 - 1) / (kTT / 32);
-    return unsigned(std::max<uint64_t>(1, std::min<uint64_t>(blocks, uint64_t(kSMs) * 16)));
+    return unsigned(std::max<uint64_t>(1, std::min<uint64_t>(blocks, uint64_t(num_sms()) * 16)));
 }
 
 }  // namespace
@@ -125,14 +125,14 @@ void readback(void* host, const void* dev, uint64_t bytes, bool kernel, cudaStre
         HJ_CUDA(cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, st));
         return;
     }
-    const unsigned grid = unsigned(std::max<uint64_t>(1, std::min<uint64_t>((bytes / 4 + kTT - 1) / kTT, uint64_t(kSMs))));
+    const unsigned grid = unsigned(std::max<uint64_t>(1, std::min<uint64_t>((bytes / 4 + kTT - 1) / kTT, uint64_t(num_sms()))));
     k_readback<<<grid, kTT, 0, st>>>(static_cast<const uint8_t*>(dev), static_cast<uint8_t*>(host), bytes);
     HJ_LAUNCH_CHECK();
 }
 
 void launch_page_headers(const uint8_t* pages, uint64_t n, uint16_t* nr, uint16_t* nn, cudaStream_t st) {
     if (n == 0) return;
-    const unsigned grid = unsigned(std::max<uint64_t>(1, std::min<uint64_t>((n + kTT - 1) / kTT, uint64_t(kSMs) * 4)));
+    const unsigned grid = unsigned(std::max<uint64_t>(1, std::min<uint64_t>((n + kTT - 1) / kTT, uint64_t(num_sms()) * 4)));
     k_page_headers<<<grid, kTT, 0, st>>>(pages, n, nr, nn);
     HJ_LAUNCH_CHECK();
 }

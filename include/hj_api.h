@@ -215,6 +215,12 @@ int  hj_result_stats(const hj_result* res, uint64_t* build_tuples, uint64_t* pro
  * "materialize", "total".
  * Phase "launches" gives the number of kernels that hj_execute launched. */
 int  hj_result_phase_ms(const hj_result* res, const char* phase, double* ms);
+/* Counters of the hj_execute that made `res`, summed over its joins (no
+ * counterpart in the reference; they size the roofline of a run):
+ * "dir_words" (directory words of the built tables, 2^b + 1 each),
+ * "table_tuples" (tuples inserted, i.e. non-NULL build keys), "joins",
+ * "launches" (kernels launched).  HJ_ERR_INVALID for another name. */
+int  hj_result_counter(const hj_result* res, const char* name, uint64_t* value);
 void hj_result_free(hj_result* res);
 
 /* ---- hash table on device columns (UnchainedHash semantics) -------------- */
@@ -251,8 +257,11 @@ void hj_table_free(hj_hash_table* t);
  * nothing.  At most HJ_NOALLOC_MAX_PROBE_ROWS probe rows per call (more:
  * HJ_ERR_INVALID with a message naming the limit).  The first call on a device
  * looks up the array's device address and should come before any stream
- * capture.  All calls share the array: calls whose GPU work overlaps race, so
- * the caller serialises them. */
+ * capture.  The address is looked up in the device's primary context (the
+ * one the CUDA runtime uses) and kept for the life of the process: calls from
+ * a non-primary driver-API context, or after cudaDeviceReset on that device,
+ * are not supported.  All calls share the array: calls whose GPU work overlaps
+ * race, so the caller serialises them. */
 #define HJ_NOALLOC_MAX_PROBE_ROWS 65536u
 #define HJ_NOALLOC_SCRATCH_BYTES (6u << 20)
 int hj_table_probe_noalloc(hj_context* ctx, const hj_hash_table* t, const int32_t* keys,

@@ -74,6 +74,10 @@ def port() -> C.CDLL:
         L.oracle_checksum.restype = u64
         L.oracle_unchained_directory.argtypes = [vp, u64, vp, u64, C.POINTER(u64)]
         L.oracle_unchained_counts.argtypes = [vp, u64, vp, u64, vp]
+        L.oracle_last_stats.argtypes = [C.POINTER(u64), C.POINTER(u64), C.POINTER(C.c_double)]
+        L.oracle_last_stats.restype = None
+        L.oracle_pages_from_int32.argtypes = [vp, vp, u64, vp, u64, C.POINTER(u64)]
+        L.oracle_pages_from_strings.argtypes = [vp, vp, vp, u64, vp, u64, C.POINTER(u64)]
         _port = L
     return _port
 
@@ -121,6 +125,25 @@ def run(L: C.CDLL, plan) -> Output:
     return _collect(L, r)
 
 
+def timed_execute(plan) -> dict:
+    """One restated execute() of `plan` for timing: its result pages are freed
+    uncopied.  Returns rows, build / probe tuples (summed over the joins) and
+    the seconds from the call to the finished result pages."""
+    L = port()
+    d, keep = plan.desc()
+    r = OracleResult()
+    L.oracle_execute(C.addressof(d), C.byref(r))
+    if r.status != 0:
+        err = r.error.decode(errors="replace")
+        L.oracle_result_free(C.byref(r))
+        raise RuntimeError(err)
+    b, p, sec = C.c_uint64(), C.c_uint64(), C.c_double()
+    L.oracle_last_stats(C.byref(b), C.byref(p), C.byref(sec))
+    rows = int(r.num_rows)
+    L.oracle_result_free(C.byref(r))
+    return {"rows": rows, "build_tuples": b.value, "probe_tuples": p.value, "seconds": sec.value}
+
+
 def to_columnar_ref(kind: int, values, valid=None):
     """Pages the reference's Table::to_columnar writes for one column."""
     L = ref()
@@ -136,6 +159,28 @@ def to_columnar_ref(kind: int, values, valid=None):
         L.ref_to_columnar_strings(b.ctypes.data if b.size else None, o.ctypes.data,
                                   None if m is None else m.ctypes.data, o.size - 1, C.byref(r))
     return _collect(L, r).columns[0][1]
+
+
+def page_writer(kind: str, *arrays) -> np.ndarray:
+    """Reference-format pages of one column written by the oracle's own writers
+    (pages.cpp): kind "int32" with (values, valid) or "strings" with (bytes,
+    offsets, valid).  The engine package calls this instead of its library's
+    writers once hooked in with `use_page_writer(oracle.page_writer)`."""
+    L = port()
+    n = C.c_uint64()
+    if kind == "int32":
+        v, m = arrays
+        args = (v.ctypes.data, None if m is None else m.ctypes.data, v.size)
+        fn = L.oracle_pages_from_int32
+    else:
+        b, o, m = arrays
+        args = (b.ctypes.data if b.size else None, o.ctypes.data, None if m is None else m.ctypes.data, o.size - 1)
+        fn = L.oracle_pages_from_strings
+    fn(*args, None, 0, C.byref(n))
+    pages = np.zeros((n.value, PAGE), dtype=np.uint8)
+    rc = fn(*args, pages.ctypes.data if n.value else None, n.value, C.byref(n))
+    assert rc == 0
+    return pages
 
 
 # ------------------------------------------------------------------ checker --

@@ -26,6 +26,7 @@
 //  * with one join thread the reference shifts a 64-bit hash by 64
 //    (partitioned_directory_hash.h:100,111, undefined); here partition 0 is used.
 #include <algorithm>
+#include <chrono>
 #include <array>
 #include <atomic>
 #include <cstdint>
@@ -298,6 +299,11 @@ struct PDHash {
     }
 };
 
+// Tuples the last execute() built and probed (summed over its joins), and
+// its duration without the copy into the oracle_result buffers.
+uint64_t g_build_tuples = 0, g_probe_tuples = 0;
+double   g_exec_seconds = 0;
+
 // ---- JoinAlgorithm::run (execute.cpp:26-186) ------------------------------
 Result hash_join(bool build_left, Result& left, Result& right, size_t left_attr, size_t right_attr,
                  const hj_attr* attrs, uint32_t na) {
@@ -310,6 +316,8 @@ Result hash_join(bool build_left, Result& left, Result& right, size_t left_attr,
     const size_t threads = num_threads_env();
     ColumnT&     bkey    = build[bcol];
     ColumnT&     pkey    = probe[pcol];
+    g_build_tuples += bkey.rows;
+    g_probe_tuples += pkey.rows;
 
     PDHash index;
     index.init(threads, 16);
@@ -499,6 +507,8 @@ extern "C" {
 int oracle_execute(const hj_plan_desc* plan, oracle_result* out) {
     using namespace oracle;
     std::memset(out, 0, sizeof(*out));
+    g_build_tuples = g_probe_tuples = 0;
+    const auto t0 = std::chrono::steady_clock::now();
     try {
         Result res = execute_impl(*plan, plan->root);
         const hj_node_desc& root = plan->nodes[plan->root];
@@ -507,6 +517,7 @@ int oracle_execute(const hj_plan_desc* plan, oracle_result* out) {
             if (root.attrs[c].type == HJ_INT32)        int32_to_pages(res[c], sinks[c]);
             else if (root.attrs[c].type == HJ_VARCHAR) varchar_to_pages(res[c], *plan, sinks[c]);
         }
+        g_exec_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         out->num_rows    = res.empty() ? 0 : res[0].rows;
         out->num_columns = root.num_attrs;
         out->types       = new int32_t[root.num_attrs + 1];
@@ -531,6 +542,14 @@ int oracle_execute(const hj_plan_desc* plan, oracle_result* out) {
         std::snprintf(out->error, sizeof(out->error), "%s", e.what());
     }
     return out->status;
+}
+
+// Build and probe tuples of the last oracle_execute (all joins) and its
+// duration up to the finished result pages.
+void oracle_last_stats(uint64_t* build, uint64_t* probe, double* seconds) {
+    *build   = oracle::g_build_tuples;
+    *probe   = oracle::g_probe_tuples;
+    *seconds = oracle::g_exec_seconds;
 }
 
 }  // extern "C"

@@ -49,8 +49,7 @@ def test_barrier_and_max_over_two_gloo_ranks():
 def test_reference_arm_under_torchrun_prints_one_line_from_rank_0():
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(_free_port()), "bench.py",
-           "--impl", "reference", "--gpus", "2", "--scale", "0.001", "--steps", "2", "--warmup", "1",
-           "--cpu-sample", "2000"]
+           "--impl", "reference", "--gpus", "2", "--scale", "0.001", "--steps", "2", "--warmup", "1"]
     r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
@@ -59,3 +58,32 @@ def test_reference_arm_under_torchrun_prints_one_line_from_rank_0():
     assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] > 0
     assert line["cpu_baseline"]["kind"] == "port"
     assert line["e2e"]["h2d_bytes_per_step"] == 0
+
+
+_NO_LIB = r"""
+import json, sys
+sys.path.insert(0, ".")
+import bench
+class A: pass
+a = A()
+a.workload, a.scale, a.steps, a.warmup, a.ref_budget_s = "c2", 0.001, 2, 1, 60.0
+line = bench.run_reference(a, bench.Dist())
+maps = open("/proc/self/maps").read()
+print(json.dumps({"line": line, "lib_mapped": "libhjgb300" in maps,
+                  "lib_loaded": sys.modules["hjgb300"]._lib is not None}))
+"""
+
+
+def test_reference_arm_never_loads_the_engine_library():
+    """The reference arm builds its input pages with the oracle's writers and
+    times the oracle: the engine library stays unloaded, and its config is the
+    one the GPU arm prints for the same workload."""
+    r = subprocess.run([sys.executable, "-c", _NO_LIB], cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    out = json.loads(r.stdout.strip().splitlines()[-1])
+    assert not out["lib_mapped"] and not out["lib_loaded"]
+    line = out["line"]
+    assert line["unit"] == line["e2e"]["unit"] == line["cpu_baseline"]["unit"] == "probe tuples/s"
+    assert line["config"]["workload"].startswith("c2: 16000 build")
+    assert line["config"]["probe_tuples"] > 0 and line["config"]["output_rows"] > 0
+    assert "whole workload" in line["cpu_baseline"]["sample"]

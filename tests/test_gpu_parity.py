@@ -60,7 +60,7 @@ def test_seeded_small_workloads_match_reference_checksums(engine, orc):
         assert (n, counts, str(cks)) == (g["num_rows"], g["column_rows"], g["checksum"]), name
 
 
-@pytest.mark.parametrize("name,scale", [("c1", 1.0), ("c2", 1 / 16), ("c3", 0.1), ("c2", 0.01)])
+@pytest.mark.parametrize("name,scale", [("c1", 1.0), ("c2", 1 / 16), ("c3", 0.1), ("c3", 1.0), ("c2", 0.01)])
 def test_workloads_match_oracle(engine, orc, name, scale):
     from hjgb300 import workloads
     w = getattr(workloads, name)(scale=scale)
@@ -68,6 +68,23 @@ def test_workloads_match_oracle(engine, orc, name, scale):
     if w.expected_rows >= 0:
         assert res.num_rows == w.expected_rows
     assert_same(orc, res, orc.run(orc.port(), w.plan), f"{name}@{scale}")
+
+
+def test_result_counters_describe_the_built_tables(engine, hj):
+    """hj_result_counter: the c1 build side (1M unique keys) gives one table of
+    1M tuples with UnchainedHash's next_pow2 directory, 2^20 + 1 words."""
+    from hjgb300 import workloads
+    w = workloads.c1(scale=1.0)
+    r = engine.execute_raw(w.plan)
+    try:
+        cnt = engine.counters(r)
+        b, p, o, _ = engine.stats(r)
+    finally:
+        engine.free_result(r)
+    assert cnt["joins"] == 1 and cnt["table_tuples"] == 1_000_000
+    assert cnt["dir_words"] == (1 << 20) + 1
+    assert (b, p, o) == (1_000_000, 10_000_000, 10_000_000)
+    assert cnt["launches"] > 0
 
 
 def test_c2_full_size_properties(engine, orc):

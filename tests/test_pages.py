@@ -32,6 +32,40 @@ def test_writer_matches_reference_layout(hj):
         assert got[k] == kat[k], k
 
 
+def test_oracle_writer_matches_reference_layout(orc):
+    """The oracle's own page writers (the reference arm builds its inputs with
+    them, without the engine library) are pinned to the same golden digests."""
+    mg = _mg()
+    kat = json.loads((GOLDEN / "writer_kat.json").read_text())
+    ints, valid, data, offs, svalid = mg.writer_inputs()
+    w = orc.page_writer
+    got = {
+        "int32_dense": mg.page_digest(w("int32", np.ascontiguousarray(ints, np.int32), None), 0),
+        "int32_nulls": mg.page_digest(w("int32", np.ascontiguousarray(ints, np.int32),
+                                        np.ascontiguousarray(valid, np.uint8)), 0),
+        "varchar_nulls_long": mg.page_digest(w("strings", np.ascontiguousarray(data, np.uint8),
+                                               np.ascontiguousarray(offs, np.uint64),
+                                               np.ascontiguousarray(svalid, np.uint8)), 3),
+    }
+    for k in kat:
+        assert got[k] == kat[k], k
+
+
+def test_oracle_writer_equals_library_writer(hj, orc):
+    r = np.random.default_rng(11)
+    for n in (0, 1, 1984, 1985, 30000):
+        v = r.integers(-2**31, 2**31, n, dtype=np.int64).astype(np.int32)
+        for m in (None, (r.random(n) > 0.2).astype(np.uint8)):
+            assert np.array_equal(hj.Column.int32(v, m).pages, orc.page_writer("int32", v, m))
+        lens = r.integers(0, 70, n)
+        lens[::997] = 9000
+        offs = np.zeros(n + 1, np.uint64)
+        np.cumsum(lens, out=offs[1:])
+        data = r.integers(0x20, 0x7f, int(offs[-1]), dtype=np.uint8)
+        for m in (None, (r.random(n) > 0.2).astype(np.uint8)):
+            assert np.array_equal(hj.Column.varchar(data, offs, m).pages, orc.page_writer("strings", data, offs, m))
+
+
 def test_writer_round_trip_through_oracle_reader(hj, orc):
     r = np.random.default_rng(5)
     n = 20000
