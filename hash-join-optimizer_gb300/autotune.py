@@ -10,7 +10,8 @@ the device, timed with CUDA events on the engine's stream, best of `repeats`):
     batch_load_pct   build rows per 100 buckets of a partition table (50 .. 90)
   plain path (HJ_BATCH_PLAIN, the engine's regular build / probe)
     radix_bits       MSD partition bits of the table build (0 .. 12, or -1 = automatic)
-    probe_group      threads per probe key in the write pass (1, 4, 8, 32)
+    probe_group      output rows per thread of the match writer (1, 4, 8, 32): a
+                     probe key's matches spread over count / probe_group threads
 
 The batched join gives each probe key one thread: its tables live in shared
 memory and a bucket holds under one key on average, so wider groups only add

@@ -63,10 +63,12 @@ __global__ void __launch_bounds__(kThreads)
     const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
     for (uint64_t w0 = uint64_t(blockIdx.x) * blockDim.x + (threadIdx.x & ~31u); w0 < kc.n;
          w0 += stride) {
-        int32_t    key;
-        const bool ok = load_key(kc, w0 + (threadIdx.x & 31), key);
+        int32_t        key;
+        const bool     ok  = load_key(kc, w0 + (threadIdx.x & 31), key);
+        const unsigned act = __ballot_sync(0xffffffffu, ok);
         if (ok) {
-            atomicAdd(hist + uint32_t(bucket_of(fib_hash(key), R)), 1u);
+            // lanes of one partition add once (a Zipf-heavy key fills whole warps)
+            warp_agg_atomic_add(hist, uint32_t(bucket_of(fib_hash(key), R)), act);
             ++mine;
         }
     }
@@ -131,10 +133,11 @@ __global__ void __launch_bounds__(kST, 1024 / kST)
     uint32_t okmask = 0;
 #pragma unroll
     for (int k = 0; k < kItems; ++k) {
-        const uint64_t i  = tile0 + uint64_t(k) * kST + threadIdx.x;
-        const bool     ok = load_key(kc, i, keys[k]);
-        parts[k]          = ok ? uint32_t(bucket_of(fib_hash(keys[k]), R)) : 0;
-        rank[k]           = ok ? atomicAdd(off + parts[k], 1u) : 0;
+        const uint64_t i   = tile0 + uint64_t(k) * kST + threadIdx.x;
+        const bool     ok  = load_key(kc, i, keys[k]);
+        parts[k]           = ok ? uint32_t(bucket_of(fib_hash(keys[k]), R)) : 0;
+        const unsigned act = __ballot_sync(0xffffffffu, ok);
+        rank[k]            = ok ? warp_agg_atomic_add(off, parts[k], act) : 0;
         okmask |= uint32_t(ok) << k;
     }
     __syncthreads();
@@ -360,7 +363,7 @@ constexpr int kLT = 1024;  // threads of k_bucket_local
 __global__ void __launch_bounds__(kLT, 1)
     k_bucket_local(Geo g, const uint32_t* __restrict__ part_off, const int32_t* __restrict__ tkey,
                    const uint32_t* __restrict__ trow, uint64_t* __restrict__ dir, int32_t* __restrict__ okey,
-                   uint32_t* __restrict__ orow, uint32_t* __restrict__ mixed) {
+                   uint32_t* __restrict__ orow, uint32_t* __restrict__ mixed, uint64_t* __restrict__ summary) {
     extern __shared__ uint32_t sh[];
     __shared__ uint32_t wsum[kLT / 32];
     const uint32_t nl    = 1u << g.L;
@@ -450,7 +453,37 @@ __global__ void __launch_bounds__(kLT, 1)
         } else if (threadIdx.x == 0 && mix[0]) {
             atomicOr(mixed + (gb >> 5), mix[0] << (gb & 31));
         }
+        // bucket summaries: cnt[i] is now the end of bucket i, so bucket i
+        // spans [end of bucket i - 1, cnt[i]); its first key is staged in sk
+        for (uint32_t i = threadIdx.x; i < nl; i += blockDim.x) {
+            const uint32_t b0  = i == 0 ? s : cnt[i - 1];
+            const uint32_t len = cnt[i] - b0;
+            summary[gb + i]    = len == 0 ? 0ull
+                                          : make_summary(sk[b0 - s], (blm[i >> 1] >> (16 * (i & 1))) & 0xffffu, len,
+                                                         (mix[i >> 5] >> (i & 31)) & 1u);
+        }
         __syncthreads();
+    }
+}
+
+// Bucket summaries of the partitions the chunked kernels built (the others
+// come from k_bucket_local): one block per partition.
+__global__ void __launch_bounds__(256)
+    k_bucket_summary(Geo g, const uint32_t* __restrict__ part_off, const uint64_t* __restrict__ dir,
+                     const int32_t* __restrict__ key, const uint32_t* __restrict__ mixed,
+                     uint64_t* __restrict__ summary) {
+    const uint32_t part = blockIdx.x;
+    if (fused_part(part_off, part)) return;
+    const uint32_t nl = 1u << g.L;
+    const uint64_t gb = uint64_t(part) << g.L;
+    for (uint32_t i = threadIdx.x; i < nl; i += blockDim.x) {
+        const uint64_t p   = gb + i;
+        const uint64_t d0  = __ldg(dir + p);
+        const uint32_t b0  = uint32_t(d0 >> 16);
+        const uint32_t len = uint32_t(__ldg(dir + p + 1) >> 16) - b0;
+        summary[p] = len == 0 ? 0ull
+                              : make_summary(__ldg(key + b0), uint32_t(d0) & 0xffffu, len,
+                                             (__ldg(mixed + (p >> 5)) >> (p & 31)) & 1u);
     }
 }
 
@@ -590,6 +623,7 @@ void build_table(const KeyCol& kc, int dir_bits, int radix_bits, Table& t, uint6
     t.keys                = dalloc_n<int32_t>(nv, st);
     t.rows                = dalloc_n<uint32_t>(nv, st);
     t.mixed               = dalloc_n<uint32_t>((nb + 31) / 32, st);
+    t.summary             = dalloc_n<uint64_t>(nb, st);
     uint32_t* gcnt        = dalloc_n<uint32_t>(nb, st);
     uint32_t* gbloom      = dalloc_n<uint32_t>(nb, st);
     HJ_CUDA(cudaMemsetAsync(gcnt, 0, nb * sizeof(uint32_t), st));
@@ -611,7 +645,8 @@ void build_table(const KeyCol& kc, int dir_bits, int radix_bits, Table& t, uint6
         const size_t smem = (nl + (nl + 1) / 2 + (nl + 31) / 32 + 2 * size_t(kFuseMax)) * sizeof(uint32_t);
         HJ_CUDA(cudaFuncSetAttribute(k_bucket_local, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
         k_bucket_local<<<std::min<uint32_t>(P, uint32_t(num_sms())), kLT, smem, st>>>(g, part_off, tkey, trow, t.dir,
-                                                                                t.keys, t.rows, t.mixed);
+                                                                                t.keys, t.rows, t.mixed,
+                                                                                t.summary);
         HJ_LAUNCH_CHECK();
     }
     {
@@ -624,6 +659,8 @@ void build_table(const KeyCol& kc, int dir_bits, int radix_bits, Table& t, uint6
     }
     k_bucket_mixed<<<chunks_upper, kThreads, 0, st>>>(g, chunk_off, part_off, t.dir, t.keys, t.mixed);
     HJ_LAUNCH_CHECK();
+    k_bucket_summary<<<P, 256, 0, st>>>(g, part_off, t.dir, t.keys, t.mixed, t.summary);
+    HJ_LAUNCH_CHECK();
 
     for (void* p : {(void*)d_nvalid, (void*)part_cnt, (void*)part_off, (void*)part_cursor,
                     (void*)chunk_off, (void*)tkey, (void*)trow, (void*)gcnt, (void*)gbloom})
@@ -631,7 +668,7 @@ void build_table(const KeyCol& kc, int dir_bits, int radix_bits, Table& t, uint6
 }
 
 void free_table(Table& t, cudaStream_t st) {
-    for (void* p : {(void*)t.dir, (void*)t.keys, (void*)t.rows, (void*)t.mixed})
+    for (void* p : {(void*)t.dir, (void*)t.keys, (void*)t.rows, (void*)t.mixed, (void*)t.summary})
         if (p) dfree(p, st);
     t = Table{};
 }

@@ -64,6 +64,25 @@ __host__ __device__ __forceinline__ uint32_t bloom_mask(uint64_t h) {
          | (1u << ((s >> 12) & 15));
 }
 
+// Bucket summary: the engine's probe-side companion of a directory word (the
+// directory itself keeps UnchainedHash's layout).  One 8-byte load gives the
+// probe everything a bucket of one key needs:
+//   bits  0..31  first key of the bucket's tuples (0 when empty)
+//   bits 32..47  the bucket's 16-bit Bloom tag (the directory word's low bits)
+//   bits 48..62  tuples in the bucket, saturated at kSumLenMax
+//   bit  63      the bucket holds more than one distinct key ("mixed")
+// An empty bucket's summary is 0.
+constexpr uint32_t kSumLenMax = 0x7fffu;
+
+__host__ __device__ __forceinline__ uint64_t make_summary(int32_t head, uint32_t bloom, uint32_t len, bool mixed) {
+    const uint64_t l = len < kSumLenMax ? len : kSumLenMax;
+    return uint64_t(uint32_t(head)) | (uint64_t(bloom & 0xffffu) << 32) | (l << 48) | (uint64_t(mixed) << 63);
+}
+__host__ __device__ __forceinline__ int32_t  sum_head(uint64_t w) { return int32_t(uint32_t(w)); }
+__host__ __device__ __forceinline__ uint32_t sum_bloom(uint64_t w) { return uint32_t(w >> 32) & 0xffffu; }
+__host__ __device__ __forceinline__ uint32_t sum_len(uint64_t w) { return uint32_t(w >> 48) & kSumLenMax; }
+__host__ __device__ __forceinline__ bool     sum_mixed(uint64_t w) { return (w >> 63) != 0; }
+
 __device__ __forceinline__ bool bit_valid(const uint32_t* bm, uint64_t i) {
     return bm == nullptr || ((__ldg(bm + (i >> 5)) >> (i & 31)) & 1u);
 }

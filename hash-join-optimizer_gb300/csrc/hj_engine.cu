@@ -350,7 +350,7 @@ struct hj_context {
     std::string         err;
     int64_t             dir_bits    = -1;
     int64_t             radix_bits  = -1;
-    int64_t             probe_group = 4;
+    int64_t             probe_group = 8;
     int64_t             light_max   = 32;
     int64_t             timing      = 0;
     int64_t             dir_cap_bits = 23;  // automatic directories stay <= 64 MB (L2 resident)
@@ -1105,7 +1105,7 @@ int hj_set_option(hj_context* c, const char* name, int64_t v) {
     if (n == "dir_bits") c->dir_bits = v;
     else if (n == "radix_bits") c->radix_bits = v;
     else if (n == "probe_group") {
-        if (v != 1 && v != 4 && v != 8 && v != 32) return HJ_ERR_INVALID;
+        if (v != 1 && v != 2 && v != 4 && v != 8 && v != 16 && v != 32) return HJ_ERR_INVALID;
         c->probe_group = v;
     } else if (n == "light_max") {
         if (v < 1) return HJ_ERR_INVALID;

@@ -93,6 +93,7 @@ struct Table {
     int32_t*  keys      = nullptr;  // adjacency array: keys
     uint32_t* rows      = nullptr;  // adjacency array: build row ids (index into KeyCol)
     uint32_t* mixed     = nullptr;  // bit p set: bucket p holds more than one distinct key
+    uint64_t* summary   = nullptr;  // 2^dir_bits bucket summaries (make_summary, hj_common.cuh)
 };
 
 // Builds `t` over the valid keys of `kc`.  dir_bits < 0: next_pow2(#valid).

@@ -3,55 +3,77 @@
 // Semantics of UnchainedHash::probe (include/unchained.h:220-246 of the
 // reference) applied to a column of probe keys, as the reference's probe
 // workers do (src/execute.cpp:111-165): NULL keys never match (:127-129),
-// Bloom early-reject on the directory word, then every tuple of the bucket
-// with an equal key is a match.
+// Bloom early-reject on the bucket's tag, then every tuple of the bucket with
+// an equal key is a match.
 //
-// Count pass (k_probe_count): each block walks 2048-row tiles.  A probe key
-// reads its directory word, rejects on the Bloom tag, and classifies the hit:
-//   light  bucket of <= light_max tuples (or a single tuple): counted by key
-//          compare; staged in shared memory via warp ballot/popc and flushed
-//          with ONE global atomic per tile (the reference's per-thread
-//          work-stealing counter becomes this per-block reservation);
-//   big    larger bucket whose tuples all carry one key (the per-bucket
-//          "mixed" bit is clear): the whole bucket matches or nothing does,
-//          so the count is the bucket size without reading it;
-//   mixed  larger bucket with several keys: counted by a whole block
-//          (k_mixed_count).
-// Write pass: prefix sums of the counts give each hit its output slot; light
-// hits are expanded by groups of `group` threads, big hits in 16K-tuple units
-// spread over all SMs (one Zipf-heavy key can own millions of tuples), mixed
-// hits by a block each.  Every match writes one row id per requested output
-// stream, composed through the sides' row-id vectors (late materialisation).
+// Count pass (k_probe_count).  A block walks tiles of 3968 probe rows (two
+// dense INT32 pages).  The tile's keys are staged in shared memory by bulk
+// asynchronous copies (TMA) while the previous tile is probed: whole pages
+// for a dense column read in place, else the decoded int32 / value_t array.
+// Per key the probe issues ONE global load, the bucket's 8-byte summary
+// (first key, Bloom tag, length, mixed flag; hj_common.cuh), eight keys per
+// thread in flight:
+//   miss     empty bucket, or the Bloom tag rejects the key;
+//   uniform  bucket of one key (mixed flag clear): the key matches every tuple
+//            of the bucket or none, decided by the first key; the hit is
+//            (probe row, bucket start, bucket length), the start read from the
+//            directory word for hits only;
+//   mixed    bucket of several keys: its tuples are compared, inline by the
+//            probing thread for buckets of at most light_max tuples, else by
+//            a warp or block per hit (k_mixed_count*).
+// Uniform hits are compacted with warp ballot/popc into shared memory and
+// flushed with ONE global atomic per 2048 rows (the reference's per-thread
+// work-stealing counter becomes this per-block reservation).
+//
+// Write pass.  A prefix sum of the uniform hits' lengths gives each hit its
+// first output slot.  k_write_uniform then walks the OUTPUT positions in
+// chunks of 256 x G (G outputs per thread, option probe_group): a chunk's
+// hits are located by the chunk map (k_chunk_first), each thread finds its
+// hit by binary search in shared memory and reads build rows rows[start + k]
+// consecutively, and every output row-id stream is written with coalesced
+// 16-byte stores through a shared-memory image.  Work is balanced by output
+// rows, so one Zipf-heavy key with millions of tuples spreads over all SMs.
+// Mixed hits follow the uniform ones.  Every match writes one row id per
+// requested output stream, composed through the sides' row-id vectors (late
+// materialisation).
 #include <algorithm>
 
 #include "hj_block.cuh"
 #include "hj_common.cuh"
 #include "hj_kernels.h"
+#include "hj_tma.cuh"
 
 namespace hj {
 
 namespace {
 
-constexpr int      kPT      = 256;
-constexpr int      kPI      = 8;
-constexpr int      kPTile   = kPT * kPI;
-constexpr uint32_t kSplit   = 2048;   // tuples per big-hit work unit (one warp each)
+constexpr int      kPT        = 256;                    // threads of the count kernel
+constexpr int      kStep      = 8;                      // rows per thread in flight
+constexpr uint32_t kHalf      = uint32_t(kPT) * kStep;  // rows per staging flush (2048)
+constexpr uint32_t kTileRows  = 2 * uint32_t(kDenseRows);  // 3968 rows per staged tile
+constexpr uint32_t kUncounted = 0xffffffffu;            // mixed hit still to be counted
+constexpr uint32_t kMixedWarpMax = 4096;                // mixed buckets up to this size: one warp each
+constexpr uint32_t kWaitPolls    = 1u << 20;            // bound of a staging wait (mbarrier polls)
+
+__host__ __device__ __forceinline__ uint64_t umin64(uint64_t a, uint64_t b) { return a < b ? a : b; }
+
+enum KeySrc : int { kSrcPages = 0, kSrcPlain = 1, kSrcTagged = 2, kSrcGather = 3 };
 
 struct ProbeTab {
     const uint64_t* dir;
+    const uint64_t* sum;
     const int32_t*  keys;
     const uint32_t* rows;
-    const uint32_t* mixed;
     uint32_t        b;
 };
 
 struct Lists {
-    uint32_t *l_row, *l_s, *l_cnt;
-    int32_t*  l_key;
-    uint32_t *b_row, *b_s, *b_e;
-    uint32_t *m_row, *m_s, *m_e, *m_cnt;
+    uint32_t *u_row, *u_s, *u_cnt;          // uniform hits: tuples [s, s + cnt) all match
+    uint32_t *m_row, *m_s, *m_e, *m_cnt;    // mixed hits: tuples [s, e) compared with m_key
     int32_t*  m_key;
-    unsigned long long* ctr;  // 0 n_light, 1 n_big, 2 n_mixed, 3 tot_light, 4 tot_big, 5 tot_mixed
+    // 0 uniform hits, 1 mixed hits, 2 uniform matches, 3 mixed matches,
+    // 4 staging waits that gave up (an error)
+    unsigned long long* ctr;
 };
 
 struct Outs {
@@ -68,162 +90,257 @@ __device__ __forceinline__ void emit(const Outs& outs, uint64_t pos, uint32_t pr
     }
 }
 
-__global__ void __launch_bounds__(kPT)
-    k_probe_count(ProbeTab T, KeyCol pk, int light_max, Lists Ls, uint64_t ntiles) {
-    __shared__ uint32_t s_row[kPTile], s_s[kPTile], s_cnt[kPTile];
-    __shared__ int32_t  s_key[kPTile];
-    __shared__ uint32_t s_n, s_base;
-    __shared__ unsigned long long s_red[33];
-    const unsigned lane = threadIdx.x & 31;
-    uint64_t       tot_light = 0, tot_big = 0;
-    for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        if (threadIdx.x == 0) s_n = 0;
-        __syncthreads();
-        // The lookups of a thread's kPI keys are issued phase by phase (keys,
-        // then directory words, then bucket heads) so that up to kPI
-        // independent memory accesses per thread are in flight.
-        int32_t  key[kPI];
-        bool     ok[kPI];
-        uint64_t w[kPI];
-#pragma unroll
-        for (int it = 0; it < kPI; ++it) {
-            const uint64_t j = tile * kPTile + uint64_t(it) * kPT + threadIdx.x;
-            ok[it]           = false;
-            key[it]          = 0;
-            if (j < pk.n) {
-                const uint64_t row = pk.rid ? uint64_t(__ldg(pk.rid + j)) : j;
-                ok[it]             = int_get(pk.col, row, key[it]);
-                // a filtered scan read raw: rows failing its predicate never match
-                if (pk.filt.n && ok[it]) ok[it] = filt_pass(pk.filt, row);
-            }
-        }
-#pragma unroll
-        for (int it = 0; it < kPI; ++it) {
-            w[it] = 0;
-            if (ok[it]) {
-                const uint64_t h = fib_hash(key[it]);
-                const uint64_t wd = __ldg(T.dir + bucket_of(h, T.b));
-                const uint32_t m  = bloom_mask(h);
-                w[it]             = (uint32_t(wd) & m) == m ? wd : 0;  // 0: rejected by the Bloom tag
-                ok[it]            = w[it] != 0;
-            }
-        }
-        uint32_t ends[kPI], heads[kPI], mixw[kPI];
-#pragma unroll
-        for (int it = 0; it < kPI; ++it) {
-            ends[it] = heads[it] = mixw[it] = 0;
-            if (ok[it]) {
-                const uint64_t p = bucket_of(fib_hash(key[it]), T.b);
-                ends[it]         = uint32_t(__ldg(T.dir + p + 1) >> 16);
-                heads[it]        = uint32_t(__ldg(T.keys + uint32_t(w[it] >> 16)));
-                mixw[it]         = __ldg(T.mixed + (p >> 5)) >> (p & 31);
-            }
-        }
-#pragma unroll
-        for (int it = 0; it < kPI; ++it) {
-            const uint64_t j   = tile * kPTile + uint64_t(it) * kPT + threadIdx.x;
-            int            cls = 0;  // 0 miss, 1 light, 2 big, 3 mixed
-            uint32_t       c = 0, s = 0, e = 0;
-            const int32_t  k = key[it];
-            if (ok[it]) {
-                s                 = uint32_t(w[it] >> 16);
-                e                 = ends[it];
-                const uint32_t L  = e - s;
-                const int32_t  k0 = int32_t(heads[it]);
-                if (L == 1) {
-                    c   = k0 == k;
-                    cls = c ? 1 : 0;
-                } else if (!(mixw[it] & 1u)) {
-                    c   = k0 == k ? L : 0;
-                    cls = c ? (L <= uint32_t(light_max) ? 1 : 2) : 0;
-                } else if (L <= uint32_t(light_max)) {
-                    for (uint32_t q = s; q < e; ++q) c += __ldg(T.keys + q) == k;
-                    cls = c ? 1 : 0;
-                } else {
-                    cls = 3;
-                }
-            }
-            const int32_t key = k;
-            // light: stage in shared memory
-            {
-                const unsigned bal = __ballot_sync(0xffffffffu, cls == 1);
-                uint32_t       base = 0;
-                if (lane == 0 && bal) base = atomicAdd(&s_n, uint32_t(__popc(bal)));
-                base = __shfl_sync(0xffffffffu, base, 0);
-                if (cls == 1) {
-                    const uint32_t q = base + __popc(bal & ((1u << lane) - 1));
-                    s_row[q]         = uint32_t(j);
-                    s_s[q]           = s;
-                    s_cnt[q]         = c;
-                    s_key[q]         = key;
-                    tot_light += c;
-                }
-            }
-            // big / mixed: rare, warp-aggregated global atomics
-            {
-                const unsigned bal = __ballot_sync(0xffffffffu, cls == 2);
-                if (bal) {
-                    unsigned long long base = 0;
-                    if (lane == 0) base = atomicAdd(Ls.ctr + 1, (unsigned long long)__popc(bal));
-                    base = __shfl_sync(0xffffffffu, base, 0);
-                    if (cls == 2) {
-                        const uint64_t q = base + __popc(bal & ((1u << lane) - 1));
-                        Ls.b_row[q]      = uint32_t(j);
-                        Ls.b_s[q]        = s;
-                        Ls.b_e[q]        = e;
-                        tot_big += c;
-                    }
-                }
-            }
-            {
-                const unsigned bal = __ballot_sync(0xffffffffu, cls == 3);
-                if (bal) {
-                    unsigned long long base = 0;
-                    if (lane == 0) base = atomicAdd(Ls.ctr + 2, (unsigned long long)__popc(bal));
-                    base = __shfl_sync(0xffffffffu, base, 0);
-                    if (cls == 3) {
-                        const uint64_t q = base + __popc(bal & ((1u << lane) - 1));
-                        Ls.m_row[q]      = uint32_t(j);
-                        Ls.m_s[q]        = s;
-                        Ls.m_e[q]        = e;
-                        Ls.m_key[q]      = key;
-                    }
-                }
-            }
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) s_base = uint32_t(atomicAdd(Ls.ctr + 0, (unsigned long long)s_n));
-        __syncthreads();
-        const uint32_t nst = s_n, gb = s_base;
-        for (uint32_t q = threadIdx.x; q < nst; q += blockDim.x) {
-            Ls.l_row[gb + q] = s_row[q];
-            Ls.l_s[gb + q]   = s_s[q];
-            Ls.l_cnt[gb + q] = s_cnt[q];
-            Ls.l_key[gb + q] = s_key[q];
-        }
-        __syncthreads();
+// Bytes of one staged tile of each key source (0: no staging).
+__host__ __device__ constexpr uint32_t stage_bytes(int src) {
+    return src == kSrcPages    ? 2u * kPage
+         : src == kSrcPlain    ? kTileRows * 4u
+         : src == kSrcTagged   ? kTileRows * 8u
+                               : 0u;
+}
+
+// Issues the bulk copy of tile `tile` of the key column into `dst`; returns
+// the rows of the tile that the copy covers (the rest are read directly).
+template <int SRC>
+__device__ __forceinline__ uint32_t stage_tile(const KeyCol& pk, uint64_t tile, uint8_t* dst, uint64_t* bar) {
+    const uint64_t r0    = tile * kTileRows;
+    const uint32_t nrows = uint32_t(umin64(kTileRows, pk.n - r0));
+    uint32_t       bytes = 0, covered = 0;
+    const void*    src   = nullptr;
+    if (SRC == kSrcPages) {
+        const uint64_t npages = (pk.n + kDenseRows - 1) / kDenseRows;
+        const uint64_t p0     = r0 / kDenseRows;
+        bytes   = uint32_t(umin64(2, npages - p0)) * kPage;
+        src     = pk.col.pages + p0 * kPage;
+        covered = nrows;
+    } else if (SRC == kSrcPlain) {
+        covered = nrows & ~3u;
+        bytes   = covered * 4u;
+        src     = pk.col.plain + r0;
+    } else {
+        covered = nrows & ~1u;
+        bytes   = covered * 8u;
+        src     = pk.col.tagged + r0;
     }
-    unsigned long long t1, t2;
-    block_exclusive_scan<unsigned long long>(tot_light, s_red, &t1);
-    block_exclusive_scan<unsigned long long>(tot_big, s_red, &t2);
-    if (threadIdx.x == 0) {
-        if (t1) atomicAdd(Ls.ctr + 3, t1);
-        if (t2) atomicAdd(Ls.ctr + 4, t2);
+    fence_proxy_async_smem();
+    mbar_arrive_expect(bar, bytes);
+    if (bytes) bulk_load(dst, src, bytes, bar);
+    return covered;
+}
+
+// Key of tile row i (row r of the key column); false for NULL.
+template <int SRC>
+__device__ __forceinline__ bool tile_key(const KeyCol& pk, const uint8_t* stage, uint32_t covered, uint32_t i,
+                                         uint64_t r, int32_t& key) {
+    if (SRC == kSrcPages) {
+        const uint32_t pl = i / kDenseRows;
+        key = reinterpret_cast<const int32_t*>(stage + size_t(pl) * kPage + 4)[i - pl * kDenseRows];
+        return true;
+    } else if (SRC == kSrcPlain) {
+        key = i < covered ? reinterpret_cast<const int32_t*>(stage)[i] : __ldg(pk.col.plain + r);
+        return bit_valid(pk.col.valid, r);
+    } else if (SRC == kSrcTagged) {
+        const uint64_t t = i < covered ? reinterpret_cast<const uint64_t*>(stage)[i] : __ldg(pk.col.tagged + r);
+        key              = int32_t(uint32_t(t));
+        return (t >> 62) == 1;
+    } else {
+        const uint64_t row = pk.rid ? uint64_t(__ldg(pk.rid + r)) : r;
+        bool           ok  = int_get(pk.col, row, key);
+        // a filtered scan read raw: rows failing its predicate never match
+        if (pk.filt.n && ok) ok = filt_pass(pk.filt, row);
+        return ok;
     }
 }
 
-// Grid of the count pass: up to 8 blocks of 256 threads per SM, looping over
-// the tiles (measured faster than a register-capped single resident wave).
-int probe_count_grid(uint64_t ntiles) {
-    return int(std::max<uint64_t>(1, std::min<uint64_t>(ntiles, uint64_t(num_sms()) * 8)));
+template <int SRC>
+__global__ void __launch_bounds__(kPT)
+    k_probe_count(ProbeTab T, KeyCol pk, int light_max, Lists Ls, uint64_t ntiles) {
+    extern __shared__ __align__(128) uint8_t dyn[];
+    constexpr uint32_t SB   = stage_bytes(SRC);
+    uint8_t*           stg  = dyn;                                            // 2 stages
+    uint32_t*          s_row = reinterpret_cast<uint32_t*>(dyn + 2 * SB);     // kHalf each
+    uint32_t*          s_s   = s_row + kHalf;
+    uint32_t*          s_cnt = s_s + kHalf;
+    __shared__ uint64_t bar[2];
+    __shared__ uint32_t s_n, s_base, s_fail, s_cov;
+    __shared__ unsigned long long s_red[33];
+    const unsigned lane = threadIdx.x & 31;
+    uint64_t       tot_u = 0, tot_m = 0;
+    uint32_t       cov0 = 0, cov1 = 0;   // thread 0: rows each stage's copy covers
+    uint32_t       iss0 = 0, iss1 = 0;   // thread 0: copies issued into each stage
+    if (threadIdx.x == 0) {
+        s_n = 0;
+        s_fail = 0;
+        if (SRC != kSrcGather) {
+            mbar_init(&bar[0]);
+            mbar_init(&bar[1]);
+        }
+    }
+    __syncthreads();
+    if (SRC != kSrcGather && threadIdx.x == 0 && uint64_t(blockIdx.x) < ntiles) {
+        cov0 = stage_tile<SRC>(pk, blockIdx.x, stg, &bar[0]);
+        iss0 = 1;
+    }
+    uint32_t k = 0;
+    for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++k) {
+        const uint32_t st = k & 1;
+        if (SRC != kSrcGather) {
+            // the other stage was last read before the previous iteration's
+            // closing barrier: refill it with the next tile now
+            const uint64_t next = tile + gridDim.x;
+            if (threadIdx.x == 0 && next < ntiles) {
+                const uint32_t c = stage_tile<SRC>(pk, next, stg + (st ^ 1) * SB, &bar[st ^ 1]);
+                if (st) { cov0 = c; ++iss0; } else { cov1 = c; ++iss1; }
+            }
+            if (!mbar_wait_bounded(&bar[st], (k >> 1) & 1, kWaitPolls)) s_fail = 1;
+            // thread 0 holds the covered counts; every thread needs this tile's
+            if (threadIdx.x == 0) s_cov = st ? cov1 : cov0;
+            __syncthreads();
+            if (s_fail) break;
+        }
+        const uint32_t cov   = SRC != kSrcGather ? s_cov : 0u;
+        const uint64_t r0    = tile * kTileRows;
+        const uint32_t nrows = uint32_t(umin64(kTileRows, pk.n - r0));
+        const uint8_t* stage = stg + st * SB;
+        for (uint32_t base = 0; base < nrows; base += kHalf) {
+            int32_t  key[kStep];
+            bool     ok[kStep];
+            uint64_t w[kStep];
+#pragma unroll
+            for (int it = 0; it < kStep; ++it) {
+                const uint32_t i = base + uint32_t(it) * kPT + threadIdx.x;
+                ok[it]           = false;
+                key[it]          = 0;
+                w[it]            = 0;
+                if (i < nrows) ok[it] = tile_key<SRC>(pk, stage, cov, i, r0 + i, key[it]);
+                if (ok[it]) w[it] = __ldg(T.sum + bucket_of(fib_hash(key[it]), T.b));
+            }
+            // classify; the directory words (bucket start, and the end of a
+            // saturated or mixed bucket) are loaded for hits only
+            uint32_t s[kStep], e[kStep];
+            int      cls[kStep];  // 0 miss, 1 uniform, 2 mixed
+#pragma unroll
+            for (int it = 0; it < kStep; ++it) {
+                const uint64_t h = fib_hash(key[it]);
+                const uint32_t m = bloom_mask(h);
+                const uint32_t L = sum_len(w[it]);
+                cls[it]          = 0;
+                if (ok[it] && L != 0 && (sum_bloom(w[it]) & m) == m)
+                    cls[it] = sum_mixed(w[it]) ? 2 : (sum_head(w[it]) == key[it] ? 1 : 0);
+                s[it] = e[it] = 0;
+                if (cls[it]) {
+                    const uint64_t p = bucket_of(h, T.b);
+                    s[it]            = uint32_t(__ldg(T.dir + p) >> 16);
+                    e[it]            = (cls[it] == 2 || L == kSumLenMax) ? uint32_t(__ldg(T.dir + p + 1) >> 16)
+                                                                         : s[it] + L;
+                }
+            }
+#pragma unroll
+            for (int it = 0; it < kStep; ++it) {
+                const uint32_t i = base + uint32_t(it) * kPT + threadIdx.x;
+                const uint64_t j = r0 + i;
+                // uniform: staged in shared memory in lane order
+                {
+                    const unsigned bal = __ballot_sync(0xffffffffu, cls[it] == 1);
+                    uint32_t       q0  = 0;
+                    if (lane == 0 && bal) q0 = atomicAdd(&s_n, uint32_t(__popc(bal)));
+                    q0 = __shfl_sync(0xffffffffu, q0, 0);
+                    if (cls[it] == 1) {
+                        const uint32_t q = q0 + __popc(bal & ((1u << lane) - 1));
+                        s_row[q]         = uint32_t(j);
+                        s_s[q]           = s[it];
+                        s_cnt[q]         = e[it] - s[it];
+                        tot_u += e[it] - s[it];
+                    }
+                }
+                // mixed: small buckets counted here, the rest later; rare, so
+                // warp-aggregated global atomics
+                uint32_t c = kUncounted;
+                if (cls[it] == 2 && e[it] - s[it] <= uint32_t(light_max)) {
+                    c = 0;
+                    for (uint32_t q = s[it]; q < e[it]; ++q) c += __ldg(T.keys + q) == key[it];
+                    if (c == 0) cls[it] = 0;
+                    tot_m += c;
+                }
+                const unsigned bal = __ballot_sync(0xffffffffu, cls[it] == 2);
+                if (bal) {
+                    unsigned long long q0 = 0;
+                    if (lane == 0) q0 = atomicAdd(Ls.ctr + 1, (unsigned long long)__popc(bal));
+                    q0 = __shfl_sync(0xffffffffu, q0, 0);
+                    if (cls[it] == 2) {
+                        const uint64_t q = q0 + __popc(bal & ((1u << lane) - 1));
+                        Ls.m_row[q]      = uint32_t(j);
+                        Ls.m_s[q]        = s[it];
+                        Ls.m_e[q]        = e[it];
+                        Ls.m_key[q]      = key[it];
+                        Ls.m_cnt[q]      = c;
+                    }
+                }
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                s_base = s_n ? uint32_t(atomicAdd(Ls.ctr + 0, (unsigned long long)s_n)) : 0u;
+            }
+            __syncthreads();
+            const uint32_t nst = s_n, gb = s_base;
+            for (uint32_t q = threadIdx.x; q < nst; q += blockDim.x) {
+                Ls.u_row[gb + q] = s_row[q];
+                Ls.u_s[gb + q]   = s_s[q];
+                Ls.u_cnt[gb + q] = s_cnt[q];
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) s_n = 0;
+            __syncthreads();
+        }
+    }
+    if (SRC != kSrcGather) {
+        // a block that gave up waits (bounded) for the copies it issued, so no
+        // copy lands in shared memory after the block has exited
+        if (s_fail && threadIdx.x == 0) {
+            atomicAdd(Ls.ctr + 4, 1ull);
+            if (iss0) mbar_wait_bounded(&bar[0], (iss0 - 1) & 1, kWaitPolls);
+            if (iss1) mbar_wait_bounded(&bar[1], (iss1 - 1) & 1, kWaitPolls);
+        }
+    }
+    unsigned long long t1, t2;
+    block_exclusive_scan<unsigned long long>(tot_u, s_red, &t1);
+    block_exclusive_scan<unsigned long long>(tot_m, s_red, &t2);
+    if (threadIdx.x == 0) {
+        if (t1) atomicAdd(Ls.ctr + 2, t1);
+        if (t2) atomicAdd(Ls.ctr + 3, t2);
+    }
+}
+
+// Mixed hits still uncounted: a warp each for buckets of up to kMixedWarpMax
+// tuples, a block each above.
+__global__ void __launch_bounds__(256) k_mixed_count_warp(ProbeTab T, Lists Ls) {
+    const uint64_t n    = Ls.ctr[1];
+    const unsigned lane = threadIdx.x & 31;
+    const uint64_t gw   = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nw   = (uint64_t(gridDim.x) * blockDim.x) >> 5;
+    unsigned long long acc = 0;
+    for (uint64_t q = gw; q < n; q += nw) {
+        if (Ls.m_cnt[q] != kUncounted) continue;
+        const uint32_t s = Ls.m_s[q], e = Ls.m_e[q];
+        if (e - s > kMixedWarpMax) continue;
+        const int32_t key = Ls.m_key[q];
+        uint32_t      c   = 0;
+        for (uint32_t i = s + lane; i < e; i += 32) c += __ldg(T.keys + i) == key;
+        c = warp_sum(c);
+        if (lane == 0) {
+            Ls.m_cnt[q] = c;
+            acc += c;
+        }
+    }
+    if (lane == 0 && acc) atomicAdd(Ls.ctr + 3, acc);
 }
 
 __global__ void __launch_bounds__(512) k_mixed_count(ProbeTab T, Lists Ls) {
     __shared__ unsigned long long s_red[33];
-    const uint64_t n   = Ls.ctr[2];
+    const uint64_t n   = Ls.ctr[1];
     uint64_t       acc = 0;
     for (uint64_t q = blockIdx.x; q < n; q += gridDim.x) {
         const uint32_t s = Ls.m_s[q], e = Ls.m_e[q];
+        if (e - s <= kMixedWarpMax || Ls.m_cnt[q] != kUncounted) continue;
         const int32_t  key = Ls.m_key[q];
         unsigned long long c = 0;
         for (uint32_t k = s + threadIdx.x; k < e; k += blockDim.x) c += __ldg(T.keys + k) == key;
@@ -234,116 +351,112 @@ __global__ void __launch_bounds__(512) k_mixed_count(ProbeTab T, Lists Ls) {
             acc += tot;
         }
     }
-    if (threadIdx.x == 0 && acc) atomicAdd(Ls.ctr + 5, (unsigned long long)acc);
+    if (threadIdx.x == 0 && acc) atomicAdd(Ls.ctr + 3, (unsigned long long)acc);
 }
 
-__global__ void k_big_units(const uint32_t* __restrict__ b_s, const uint32_t* __restrict__ b_e,
-                            uint64_t n, uint32_t* __restrict__ units, uint32_t* __restrict__ lens) {
-    const uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const uint32_t L = b_e[i] - b_s[i];
-    lens[i]          = L;
-    units[i]         = (L + kSplit - 1) / kSplit;
+// Largest h < n with off[h] <= x (off non-decreasing, off[0] = 0).
+__device__ __forceinline__ uint64_t hit_of(const uint64_t* __restrict__ off, uint64_t n, uint64_t x) {
+    uint64_t lo = 0, hi = n;
+    while (hi - lo > 1) {
+        const uint64_t mid = (lo + hi) >> 1;
+        if (__ldg(off + mid) <= x) lo = mid;
+        else                       hi = mid;
+    }
+    return lo;
 }
+
+// chunk_first[c] = the uniform hit holding output position c * chunk.
+__global__ void k_chunk_first(const uint64_t* __restrict__ off, uint64_t n_u, uint64_t nchunks, uint32_t chunk,
+                              uint32_t* __restrict__ chunk_first) {
+    const uint64_t c = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (c < nchunks) chunk_first[c] = uint32_t(hit_of(off, n_u, c * chunk));
+}
+
+// Shared memory of k_write_uniform<G>: hit offsets, tuple bases and probe rows
+// of a chunk's hits (up to chunk + 1 each) plus one output stream's image.
+constexpr size_t write_uniform_smem(int G) { return (4 * (size_t(256) * G) + 4) * sizeof(uint32_t); }
+// (a chunk of CH outputs has at most CH + 1 hits: every hit holds at least one
+// output, plus the hit that starts at the next chunk's first position)
 
 template <int G>
 __global__ void __launch_bounds__(256)
-    k_write_light(ProbeTab T, Lists Ls, uint64_t n_light, const uint64_t* __restrict__ off, Outs outs) {
-    const unsigned lane = threadIdx.x & 31;
-    const unsigned grp  = lane / G, gl = lane % G;
-    const unsigned gmask = G == 32 ? 0xffffffffu : ((1u << G) - 1) << (grp * G);
-    const uint64_t warp   = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-    const uint64_t nwarps = (uint64_t(gridDim.x) * blockDim.x) >> 5;
-    constexpr int  HPW    = 32 / G;  // hits per warp step
-    for (uint64_t hb = warp * HPW; hb < n_light; hb += nwarps * HPW) {
-        const uint64_t h    = hb + grp;
-        const bool     have = h < n_light;
-        uint32_t       s = 0, L = 0, prow = 0;
-        int32_t        key = 0;
-        uint64_t       pos = 0;
-        bool mixed = false;
-        if (have) {
-            s    = Ls.l_s[h];
-            prow = Ls.l_row[h];
-            key  = Ls.l_key[h];
-            pos  = off[h];
-            // a bucket of one key matches whole: its length is the count (the
-            // mixed bitmap, 1 bit per bucket, stays in L2); a mixed bucket's end
-            // is the next directory word's start
-            const uint64_t p = bucket_of(fib_hash(key), T.b);
-            mixed            = (__ldg(T.mixed + (p >> 5)) >> (p & 31)) & 1u;
-            L                = mixed ? uint32_t(__ldg(T.dir + p + 1) >> 16) - s : Ls.l_cnt[h];
+    k_write_uniform(ProbeTab T, Lists Ls, uint64_t n_u, const uint64_t* __restrict__ off,
+                    const uint32_t* __restrict__ chunk_first, uint64_t total, Outs outs) {
+    constexpr uint32_t CH = 256u * G;
+    extern __shared__ __align__(16) uint32_t wsh[];
+    uint32_t* s_rel = wsh;               // CH + 2: hit starts relative to the chunk, clamped to [0, len]
+    uint32_t* s_tb  = s_rel + CH + 2;    // CH + 1: tuple index of the chunk's position 0 within each hit
+    uint32_t* s_pr  = s_tb + CH + 1;     // CH + 1: probe row of each hit
+    uint32_t* s_val = s_pr + CH + 1;     // CH: one output stream (16-byte aligned: 3 CH + 4 words in)
+    __shared__ uint64_t s_h[2];
+    const uint64_t nchunks = (total + CH - 1) / CH;
+    for (uint64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+        const uint64_t o0  = c * CH;
+        const uint32_t len = uint32_t(umin64(CH, total - o0));
+        if (threadIdx.x == 0) {
+            s_h[0] = chunk_first ? chunk_first[c] : hit_of(off, n_u, o0);
+            s_h[1] = c + 1 < nchunks ? (chunk_first ? chunk_first[c + 1] : hit_of(off, n_u, o0 + CH)) : n_u - 1;
         }
-        for (uint32_t k0 = 0; __any_sync(0xffffffffu, have && k0 < L); k0 += G) {
-            const uint32_t k   = s + k0 + gl;
-            const bool     in  = have && k0 + gl < L;
-            const uint32_t row = in ? __ldg(T.rows + k) : 0u;  // loaded beside the key
-            const bool     m   = in && (!mixed || __ldg(T.keys + k) == key);
-            const unsigned bl  = __ballot_sync(0xffffffffu, m) & gmask;
-            if (m) emit(outs, pos + __popc(bl & ((1u << lane) - 1)), prow, row);
-            pos += __popc(bl);
+        __syncthreads();
+        const uint64_t h0 = s_h[0];
+        const uint32_t nh = uint32_t(s_h[1] - h0) + 1;  // hits h0 .. h0 + nh - 1 cover the chunk
+        for (uint32_t q = threadIdx.x; q <= nh; q += blockDim.x) {
+            const uint64_t o   = __ldg(off + h0 + q);
+            const uint64_t rel = o > o0 ? o - o0 : 0;
+            s_rel[q]           = uint32_t(umin64(rel, len));
+            if (q < nh) {
+                s_pr[q] = __ldg(Ls.u_row + h0 + q);
+                s_tb[q] = __ldg(Ls.u_s + h0 + q) - uint32_t(o - o0);  // mod 2^32: start - (offset - o0)
+            }
         }
-    }
-}
-
-// unit_hit[u] = the big hit that work unit u belongs to.
-__global__ void k_unit_map(const uint64_t* __restrict__ unit_off, uint64_t n_big, uint32_t* __restrict__ unit_hit) {
-    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
-    for (uint64_t h = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; h < n_big; h += stride)
-        for (uint64_t u = unit_off[h]; u < unit_off[h + 1]; ++u) unit_hit[u] = uint32_t(h);
-}
-
-__global__ void __launch_bounds__(256)
-    k_write_big(ProbeTab T, Lists Ls, uint64_t n_big, const uint64_t* __restrict__ unit_off,
-                const uint32_t* __restrict__ unit_hit, const uint64_t* __restrict__ big_off, uint64_t base_pos,
-                Outs outs) {
-    // one warp per unit: most big hits are a few hundred tuples, so a whole
-    // block per unit would leave most of its lanes idle
-    const uint64_t nunits = unit_off[n_big];
-    const unsigned lane   = threadIdx.x & 31;
-    const uint64_t gw     = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-    const uint64_t nw     = (uint64_t(gridDim.x) * blockDim.x) >> 5;
-    for (uint64_t u = gw; u < nunits; u += nw) {
-        uint64_t h;
-        if (unit_hit) {
-            h = unit_hit[u];
-        } else {  // no map: largest h with unit_off[h] <= u
-            uint64_t lo = 0, hi = n_big;
+        __syncthreads();
+        const uint32_t q0 = threadIdx.x * G;
+        uint32_t       prow[G], brow[G];
+        if (q0 < len) {
+            uint32_t lo = 0, hi = nh;  // largest k with s_rel[k] <= q0
             while (hi - lo > 1) {
-                const uint64_t mid = (lo + hi) >> 1;
-                if (unit_off[mid] <= u) lo = mid;
-                else                    hi = mid;
+                const uint32_t mid = (lo + hi) >> 1;
+                if (s_rel[mid] <= q0) lo = mid;
+                else                  hi = mid;
             }
-            h = lo;
+            uint32_t k = lo;
+#pragma unroll
+            for (int i = 0; i < G; ++i) {
+                const uint32_t q = q0 + i;
+                if (q < len) {
+                    while (s_rel[k + 1] <= q) ++k;
+                    prow[i] = s_pr[k];
+                    brow[i] = __ldg(T.rows + (s_tb[k] + q));
+                }
+            }
         }
-        const uint64_t sub  = u - unit_off[h];
-        const uint32_t s0   = Ls.b_s[h] + uint32_t(sub) * kSplit;
-        const uint32_t e0   = min(Ls.b_e[h], s0 + kSplit);
-        const uint32_t prow = Ls.b_row[h];
-        const uint64_t pos0 = base_pos + big_off[h] + sub * kSplit;
-        // four loads per lane in flight, then their outputs
-        for (uint32_t k0 = s0; k0 < e0; k0 += 128) {
-            uint32_t r[4];
+        for (int oi = 0; oi < outs.n; ++oi) {
+            const RidOut o = outs.o[oi];
+            if (q0 < len) {
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const uint32_t k = k0 + 32u * q + lane;
-                r[q]             = k < e0 ? __ldg(T.rows + k) : 0u;
+                for (int i = 0; i < G; ++i) {
+                    if (q0 + i < len) {
+                        const uint32_t x = o.side == 0 ? prow[i] : brow[i];
+                        s_val[q0 + i]    = o.src ? __ldg(o.src + x) : x;
+                    }
+                }
             }
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const uint32_t k = k0 + 32u * q + lane;
-                if (k < e0) emit(outs, pos0 + (k - s0), prow, r[q]);
-            }
+            __syncthreads();
+            uint32_t*      dst = o.dst + o0;
+            // 16-byte stores where the caller's buffer allows (engine buffers always do)
+            const uint32_t n4  = (reinterpret_cast<uintptr_t>(dst) & 15) ? 0u : len / 4;
+            for (uint32_t v = threadIdx.x; v < n4; v += blockDim.x)
+                reinterpret_cast<uint4*>(dst)[v] = reinterpret_cast<const uint4*>(s_val)[v];
+            for (uint32_t v = 4 * n4 + threadIdx.x; v < len; v += blockDim.x) dst[v] = s_val[v];
+            __syncthreads();
         }
     }
 }
-
-constexpr uint32_t kMixedWarpMax = 4096;  // mixed buckets up to this size: one warp each
 
 __global__ void __launch_bounds__(256)
     k_write_mixed_warp(ProbeTab T, Lists Ls, const uint64_t* __restrict__ mixed_off, uint64_t base_pos,
                        Outs outs) {
-    const uint64_t n    = Ls.ctr[2];
+    const uint64_t n    = Ls.ctr[1];
     const unsigned lane = threadIdx.x & 31;
     const uint64_t gw   = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     const uint64_t nw   = (uint64_t(gridDim.x) * blockDim.x) >> 5;
@@ -367,7 +480,7 @@ __global__ void __launch_bounds__(512)
     k_write_mixed(ProbeTab T, Lists Ls, const uint64_t* __restrict__ mixed_off, uint64_t base_pos,
                   Outs outs) {
     __shared__ uint32_t sm[33];
-    const uint64_t n = Ls.ctr[2];
+    const uint64_t n = Ls.ctr[1];
     for (uint64_t q = blockIdx.x; q < n; q += gridDim.x) {
         const uint32_t s = Ls.m_s[q], e = Ls.m_e[q], prow = Ls.m_row[q];
         if (e - s <= kMixedWarpMax) continue;  // done by k_write_mixed_warp
@@ -384,15 +497,99 @@ __global__ void __launch_bounds__(512)
     }
 }
 
-ProbeTab tab_of(const Table& t) { return ProbeTab{t.dir, t.keys, t.rows, t.mixed, t.dir_bits}; }
+ProbeTab tab_of(const Table& t) { return ProbeTab{t.dir, t.summary, t.keys, t.rows, t.dir_bits}; }
+
+int key_source(const KeyCol& pk) {
+    if (pk.rid || pk.filt.n) return kSrcGather;
+    if (pk.col.tagged) return kSrcTagged;
+    if (pk.col.plain) return kSrcPlain;
+    return kSrcPages;
+}
+
+template <int SRC>
+void launch_count_src(const ProbeTab& T, const KeyCol& pk, int light_max, const Lists& L, cudaStream_t st) {
+    const uint64_t ntiles = (pk.n + kTileRows - 1) / kTileRows;
+    const size_t   smem   = 2 * size_t(stage_bytes(SRC)) + 3 * size_t(kHalf) * sizeof(uint32_t);
+    HJ_CUDA(cudaFuncSetAttribute(k_probe_count<SRC>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    // resident blocks walk the tiles (each prefetching its next tile)
+    int per_sm = 0;
+    HJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_probe_count<SRC>, kPT, smem));
+    const uint64_t grid = std::max<uint64_t>(1, std::min<uint64_t>(ntiles, uint64_t(num_sms()) * std::max(1, per_sm)));
+    k_probe_count<SRC><<<unsigned(grid), kPT, smem, st>>>(T, pk, light_max, L, ntiles);
+    HJ_LAUNCH_CHECK();
+}
+
+// Count kernels over a probe column: uniform and mixed lists, counters in L.ctr.
+void launch_count(const ProbeTab& T, const KeyCol& pk, int light_max, const Lists& L, cudaStream_t st) {
+    switch (key_source(pk)) {
+    case kSrcPages: launch_count_src<kSrcPages>(T, pk, light_max, L, st); break;
+    case kSrcPlain: launch_count_src<kSrcPlain>(T, pk, light_max, L, st); break;
+    case kSrcTagged: launch_count_src<kSrcTagged>(T, pk, light_max, L, st); break;
+    default: launch_count_src<kSrcGather>(T, pk, light_max, L, st); break;
+    }
+    k_mixed_count_warp<<<num_sms() * 4, 256, 0, st>>>(T, L);
+    HJ_LAUNCH_CHECK();
+    k_mixed_count<<<num_sms() * 2, 512, 0, st>>>(T, L);
+    HJ_LAUNCH_CHECK();
+}
+
+// Outputs per thread of the uniform writer from option probe_group.
+int writer_items(int group) {
+    switch (group) {
+    case 1: return 1;
+    case 2: return 2;
+    case 4: return 4;
+    case 16: return 16;
+    case 32: return 32;
+    default: return 8;
+    }
+}
+
+template <int G>
+void launch_uniform_g(const ProbeTab& T, const Lists& L, uint64_t n_u, const uint64_t* off, const uint32_t* chunk_first,
+                      uint64_t total, const Outs& outs, cudaStream_t st) {
+    const size_t smem = write_uniform_smem(G);
+    HJ_CUDA(cudaFuncSetAttribute(k_write_uniform<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    int per_sm = 0;
+    HJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_write_uniform<G>, 256, smem));
+    const uint64_t nchunks = (total + 256u * G - 1) / (256u * G);
+    const uint64_t grid    = std::max<uint64_t>(1, std::min<uint64_t>(nchunks, uint64_t(num_sms()) * std::max(1, per_sm)));
+    k_write_uniform<G><<<unsigned(grid), 256, smem, st>>>(T, L, n_u, off, chunk_first, total, outs);
+    HJ_LAUNCH_CHECK();
+}
+
+void launch_uniform(int G, const ProbeTab& T, const Lists& L, uint64_t n_u, const uint64_t* off,
+                    const uint32_t* chunk_first, uint64_t total, const Outs& outs, cudaStream_t st) {
+    switch (G) {
+    case 1: launch_uniform_g<1>(T, L, n_u, off, chunk_first, total, outs, st); break;
+    case 2: launch_uniform_g<2>(T, L, n_u, off, chunk_first, total, outs, st); break;
+    case 4: launch_uniform_g<4>(T, L, n_u, off, chunk_first, total, outs, st); break;
+    case 16: launch_uniform_g<16>(T, L, n_u, off, chunk_first, total, outs, st); break;
+    case 32: launch_uniform_g<32>(T, L, n_u, off, chunk_first, total, outs, st); break;
+    default: launch_uniform_g<8>(T, L, n_u, off, chunk_first, total, outs, st); break;
+    }
+}
+
+void launch_mixed_writers(const ProbeTab& T, const Lists& L, const uint64_t* mixed_off, uint64_t base_pos,
+                          const Outs& outs, cudaStream_t st) {
+    k_write_mixed_warp<<<num_sms() * 8, 256, 0, st>>>(T, L, mixed_off, base_pos, outs);
+    HJ_LAUNCH_CHECK();
+    k_write_mixed<<<num_sms() * 2, 512, 0, st>>>(T, L, mixed_off, base_pos, outs);
+    HJ_LAUNCH_CHECK();
+}
+
+void check_staging(const uint64_t* host_ctr) {
+    if (host_ctr[4])
+        throw Error(HJ_ERR_DEVICE_STATUS, "probe: " + std::to_string(host_ctr[4])
+                                              + " blocks gave up waiting for their staged key tiles");
+}
 
 }  // namespace
 
 struct ProbePlan {
     Lists     ls{};
     uint64_t  cap     = 0;
-    uint64_t  n_light = 0, n_big = 0, n_mixed = 0;
-    uint64_t  tot_light = 0, tot_big = 0, tot_mixed = 0;
+    uint64_t  n_u = 0, n_m = 0, tot_u = 0, tot_m = 0;
     uint64_t* host    = nullptr;  // pinned readback of the counters (owned by the caller)
     int       group   = 8;
 };
@@ -407,13 +604,9 @@ uint64_t probe_count(const Table& t, const KeyCol& pk, const ProbeParams& prm, P
     const uint64_t n = pk.n;
     pp->cap          = n;
     Lists& L         = pp->ls;
-    L.l_row = dalloc_n<uint32_t>(n, st);
-    L.l_s   = dalloc_n<uint32_t>(n, st);
-    L.l_cnt = dalloc_n<uint32_t>(n, st);
-    L.l_key = dalloc_n<int32_t>(n, st);
-    L.b_row = dalloc_n<uint32_t>(n, st);
-    L.b_s   = dalloc_n<uint32_t>(n, st);
-    L.b_e   = dalloc_n<uint32_t>(n, st);
+    L.u_row = dalloc_n<uint32_t>(n, st);
+    L.u_s   = dalloc_n<uint32_t>(n, st);
+    L.u_cnt = dalloc_n<uint32_t>(n, st);
     L.m_row = dalloc_n<uint32_t>(n, st);
     L.m_s   = dalloc_n<uint32_t>(n, st);
     L.m_e   = dalloc_n<uint32_t>(n, st);
@@ -421,24 +614,17 @@ uint64_t probe_count(const Table& t, const KeyCol& pk, const ProbeParams& prm, P
     L.m_key = dalloc_n<int32_t>(n, st);
     L.ctr   = dalloc_n<unsigned long long>(8, st);
     HJ_CUDA(cudaMemsetAsync(L.ctr, 0, 8 * sizeof(unsigned long long), st));
-    const ProbeTab T      = tab_of(t);
-    const uint64_t ntiles = (n + kPTile - 1) / kPTile;
-    const int      grid   = probe_count_grid(ntiles);
-    k_probe_count<<<grid, kPT, 0, st>>>(T, pk, prm.light_max, L, ntiles);
-    HJ_LAUNCH_CHECK();
-    k_mixed_count<<<num_sms() * 2, 512, 0, st>>>(T, L);
-    HJ_LAUNCH_CHECK();
+    launch_count(tab_of(t), pk, prm.light_max, L, st);
     if (prm.after_count) prm.after_count();
     pp->host = prm.pinned;
-    readback(pp->host, L.ctr, 6 * sizeof(uint64_t), true, st);  // page-locked scratch
+    readback(pp->host, L.ctr, 5 * sizeof(uint64_t), true, st);  // page-locked scratch
     HJ_CUDA(cudaStreamSynchronize(st));
-    pp->n_light   = pp->host[0];
-    pp->n_big     = pp->host[1];
-    pp->n_mixed   = pp->host[2];
-    pp->tot_light = pp->host[3];
-    pp->tot_big   = pp->host[4];
-    pp->tot_mixed = pp->host[5];
-    return pp->tot_light + pp->tot_big + pp->tot_mixed;
+    check_staging(pp->host);
+    pp->n_u   = pp->host[0];
+    pp->n_m   = pp->host[1];
+    pp->tot_u = pp->host[2];
+    pp->tot_m = pp->host[3];
+    return pp->tot_u + pp->tot_m;
 }
 
 void probe_write(const Table& t, const KeyCol& pk, ProbePlan* pp, const RidOut* ro, int nout,
@@ -451,44 +637,23 @@ void probe_write(const Table& t, const KeyCol& pk, ProbePlan* pp, const RidOut* 
     if (pp->cap == 0 || nout == 0) return;
     const ProbeTab T = tab_of(t);
     Lists&         L = pp->ls;
-    if (pp->n_light) {
-        uint64_t* off = dalloc_n<uint64_t>(pp->n_light + 1, st);
-        scan_exclusive_u32_to_u64(L.l_cnt, off, pp->n_light, st);
-        const int grid = int(std::min<uint64_t>(div_up(pp->n_light, 256), uint64_t(num_sms()) * 16));
-        switch (pp->group) {
-        case 1: k_write_light<1><<<grid, 256, 0, st>>>(T, L, pp->n_light, off, outs); break;
-        case 4: k_write_light<4><<<grid, 256, 0, st>>>(T, L, pp->n_light, off, outs); break;
-        case 32: k_write_light<32><<<grid, 256, 0, st>>>(T, L, pp->n_light, off, outs); break;
-        default: k_write_light<8><<<grid, 256, 0, st>>>(T, L, pp->n_light, off, outs); break;
-        }
+    if (pp->n_u) {
+        const int      G       = writer_items(pp->group);
+        const uint64_t chunk   = 256u * uint64_t(G);
+        const uint64_t nchunks = (pp->tot_u + chunk - 1) / chunk;
+        uint64_t*      off     = dalloc_n<uint64_t>(pp->n_u + 1, st);
+        uint32_t*      cfirst  = dalloc_n<uint32_t>(nchunks + 1, st);
+        scan_exclusive_u32_to_u64(L.u_cnt, off, pp->n_u, st);
+        k_chunk_first<<<div_up(nchunks, 256), 256, 0, st>>>(off, pp->n_u, nchunks, uint32_t(chunk), cfirst);
         HJ_LAUNCH_CHECK();
+        launch_uniform(G, T, L, pp->n_u, off, cfirst, pp->tot_u, outs, st);
         dfree(off, st);
+        dfree(cfirst, st);
     }
-    if (pp->n_big) {
-        uint32_t* units    = dalloc_n<uint32_t>(pp->n_big, st);
-        uint32_t* lens     = dalloc_n<uint32_t>(pp->n_big, st);
-        uint64_t* unit_off = dalloc_n<uint64_t>(pp->n_big + 1, st);
-        uint64_t* big_off  = dalloc_n<uint64_t>(pp->n_big + 1, st);
-        k_big_units<<<div_up(pp->n_big, 256), 256, 0, st>>>(L.b_s, L.b_e, pp->n_big, units, lens);
-        HJ_LAUNCH_CHECK();
-        scan_exclusive_u32_to_u64(units, unit_off, pp->n_big, st);
-        scan_exclusive_u32_to_u64(lens, big_off, pp->n_big, st);
-        // every big hit has >= 1 unit and units = ceil(len / kSplit) <= 1 + len / kSplit
-        const uint64_t max_units = pp->n_big + pp->tot_big / kSplit + 1;
-        uint32_t*      unit_hit  = dalloc_n<uint32_t>(max_units, st);
-        k_unit_map<<<div_up(pp->n_big, 256), 256, 0, st>>>(unit_off, pp->n_big, unit_hit);
-        HJ_LAUNCH_CHECK();
-        k_write_big<<<num_sms() * 8, 256, 0, st>>>(T, L, pp->n_big, unit_off, unit_hit, big_off, pp->tot_light, outs);
-        HJ_LAUNCH_CHECK();
-        for (void* p : {(void*)units, (void*)lens, (void*)unit_off, (void*)big_off, (void*)unit_hit}) dfree(p, st);
-    }
-    if (pp->n_mixed) {
-        uint64_t* off = dalloc_n<uint64_t>(pp->n_mixed + 1, st);
-        scan_exclusive_u32_to_u64(L.m_cnt, off, pp->n_mixed, st);
-        k_write_mixed_warp<<<num_sms() * 8, 256, 0, st>>>(T, L, off, pp->tot_light + pp->tot_big, outs);
-        HJ_LAUNCH_CHECK();
-        k_write_mixed<<<num_sms() * 2, 512, 0, st>>>(T, L, off, pp->tot_light + pp->tot_big, outs);
-        HJ_LAUNCH_CHECK();
+    if (pp->n_m) {
+        uint64_t* off = dalloc_n<uint64_t>(pp->n_m + 1, st);
+        scan_exclusive_u32_to_u64(L.m_cnt, off, pp->n_m, st);
+        launch_mixed_writers(T, L, off, pp->tot_u, outs, st);
         dfree(off, st);
     }
 }
@@ -511,8 +676,8 @@ struct Carve {
 
 size_t probe_scratch_bytes(uint64_t n) {
     const uint64_t tmp = scan_tmp_words(n) + 1;
-    return 14 * ((4 * n + 255) & ~uint64_t(255)) + 4 * ((8 * (n + 1) + 255) & ~uint64_t(255))
-         + ((8 * tmp + 255) & ~uint64_t(255)) + 256;
+    return 256 + 8 * ((4 * n + 255) & ~uint64_t(255)) + 2 * ((8 * (n + 1) + 255) & ~uint64_t(255))
+         + ((8 * tmp + 255) & ~uint64_t(255));
 }
 
 int probe_into_scratch(const Table& t, const KeyCol& pk, const ProbeParams& prm, uint8_t* scratch,
@@ -523,43 +688,29 @@ int probe_into_scratch(const Table& t, const KeyCol& pk, const ProbeParams& prm,
     const uint64_t n = pk.n;
     if (probe_scratch_bytes(n) > scratch_bytes) throw Error(HJ_ERR_INVALID, "probe scratch too small");
     Lists     L{};
-    uint64_t *light_off, *unit_off, *big_off, *mixed_off, *tmp;
-    uint32_t *units, *lens;
+    uint64_t *u_off, *m_off, *tmp;
     Carve     c{scratch};
-    L.ctr     = c.take<unsigned long long>(8);
-    L.l_row   = c.take<uint32_t>(n);
-    L.l_s     = c.take<uint32_t>(n);
-    L.l_cnt   = c.take<uint32_t>(n);
-    L.l_key   = c.take<int32_t>(n);
-    L.b_row   = c.take<uint32_t>(n);
-    L.b_s     = c.take<uint32_t>(n);
-    L.b_e     = c.take<uint32_t>(n);
-    L.m_row   = c.take<uint32_t>(n);
-    L.m_s     = c.take<uint32_t>(n);
-    L.m_e     = c.take<uint32_t>(n);
-    L.m_cnt   = c.take<uint32_t>(n);
-    L.m_key   = c.take<int32_t>(n);
-    units     = c.take<uint32_t>(n);
-    lens      = c.take<uint32_t>(n);
-    light_off = c.take<uint64_t>(n + 1);
-    unit_off  = c.take<uint64_t>(n + 1);
-    big_off   = c.take<uint64_t>(n + 1);
-    mixed_off = c.take<uint64_t>(n + 1);
-    tmp       = c.take<uint64_t>(scan_tmp_words(n) + 1);
+    L.ctr   = c.take<unsigned long long>(8);
+    L.u_row = c.take<uint32_t>(n);
+    L.u_s   = c.take<uint32_t>(n);
+    L.u_cnt = c.take<uint32_t>(n);
+    L.m_row = c.take<uint32_t>(n);
+    L.m_s   = c.take<uint32_t>(n);
+    L.m_e   = c.take<uint32_t>(n);
+    L.m_cnt = c.take<uint32_t>(n);
+    L.m_key = c.take<int32_t>(n);
+    u_off   = c.take<uint64_t>(n + 1);
+    m_off   = c.take<uint64_t>(n + 1);
+    tmp     = c.take<uint64_t>(scan_tmp_words(n) + 1);
     // the scratch keeps the previous call's contents: the counters restart at zero
     HJ_CUDA(cudaMemsetAsync(L.ctr, 0, 8 * sizeof(unsigned long long), st));
-    const ProbeTab T      = tab_of(t);
-    const uint64_t ntiles = (n + kPTile - 1) / kPTile;
-    const int      grid   = probe_count_grid(ntiles);
-    k_probe_count<<<grid, kPT, 0, st>>>(T, pk, prm.light_max, L, ntiles);
-    HJ_LAUNCH_CHECK();
-    k_mixed_count<<<num_sms() * 2, 512, 0, st>>>(T, L);
-    HJ_LAUNCH_CHECK();
+    const ProbeTab T = tab_of(t);
+    launch_count(T, pk, prm.light_max, L, st);
     uint64_t* h = prm.pinned;
-    readback(h, L.ctr, 6 * sizeof(uint64_t), true, st);  // page-locked scratch
+    readback(h, L.ctr, 5 * sizeof(uint64_t), true, st);  // page-locked scratch
     HJ_CUDA(cudaStreamSynchronize(st));
-    const uint64_t n_light = h[0], n_big = h[1], n_mixed = h[2];
-    const uint64_t tot_light = h[3], tot_big = h[4], total = h[3] + h[4] + h[5];
+    check_staging(h);
+    const uint64_t n_u = h[0], n_m = h[1], tot_u = h[2], total = h[2] + h[3];
     *num_matches = total;
     if (total > capacity) return HJ_ERR_CAPACITY;
     if (total == 0) return HJ_OK;
@@ -567,40 +718,15 @@ int probe_into_scratch(const Table& t, const KeyCol& pk, const ProbeParams& prm,
     outs.n    = 2;
     outs.o[0] = RidOut{0, nullptr, out_probe};
     outs.o[1] = RidOut{1, nullptr, out_build};
-    if (n_light) {
-        scan_exclusive_u32_to_u64_into(L.l_cnt, light_off, n_light, tmp, st);
-        const int g = int(std::min<uint64_t>(div_up(n_light, 256), uint64_t(num_sms()) * 16));
-        switch (prm.group) {
-        case 1: k_write_light<1><<<g, 256, 0, st>>>(T, L, n_light, light_off, outs); break;
-        case 4: k_write_light<4><<<g, 256, 0, st>>>(T, L, n_light, light_off, outs); break;
-        case 32: k_write_light<32><<<g, 256, 0, st>>>(T, L, n_light, light_off, outs); break;
-        default: k_write_light<8><<<g, 256, 0, st>>>(T, L, n_light, light_off, outs); break;
-        }
-        HJ_LAUNCH_CHECK();
+    if (n_u) {
+        scan_exclusive_u32_to_u64_into(L.u_cnt, u_off, n_u, tmp, st);
+        // no chunk map (its size would follow the match count): each chunk
+        // finds its first hit by binary search
+        launch_uniform(writer_items(prm.group), T, L, n_u, u_off, nullptr, tot_u, outs, st);
     }
-    if (n_big) {
-        k_big_units<<<div_up(n_big, 256), 256, 0, st>>>(L.b_s, L.b_e, n_big, units, lens);
-        HJ_LAUNCH_CHECK();
-        scan_exclusive_u32_to_u64_into(units, unit_off, n_big, tmp, st);
-        scan_exclusive_u32_to_u64_into(lens, big_off, n_big, tmp, st);
-        // the per-hit unit counts were consumed by the scan above, so their
-        // n-entry array holds the unit map when it fits; otherwise the write
-        // kernel finds each unit's hit by binary search
-        const uint64_t max_units = n_big + h[4] / kSplit + 1;
-        uint32_t*      unit_hit  = max_units <= n ? units : nullptr;
-        if (unit_hit) {
-            k_unit_map<<<div_up(n_big, 256), 256, 0, st>>>(unit_off, n_big, unit_hit);
-            HJ_LAUNCH_CHECK();
-        }
-        k_write_big<<<num_sms() * 8, 256, 0, st>>>(T, L, n_big, unit_off, unit_hit, big_off, tot_light, outs);
-        HJ_LAUNCH_CHECK();
-    }
-    if (n_mixed) {
-        scan_exclusive_u32_to_u64_into(L.m_cnt, mixed_off, n_mixed, tmp, st);
-        k_write_mixed_warp<<<num_sms() * 8, 256, 0, st>>>(T, L, mixed_off, tot_light + tot_big, outs);
-        HJ_LAUNCH_CHECK();
-        k_write_mixed<<<num_sms() * 2, 512, 0, st>>>(T, L, mixed_off, tot_light + tot_big, outs);
-        HJ_LAUNCH_CHECK();
+    if (n_m) {
+        scan_exclusive_u32_to_u64_into(L.m_cnt, m_off, n_m, tmp, st);
+        launch_mixed_writers(T, L, m_off, tot_u, outs, st);
     }
     return HJ_OK;
 }
@@ -608,8 +734,7 @@ int probe_into_scratch(const Table& t, const KeyCol& pk, const ProbeParams& prm,
 void probe_free(ProbePlan* pp, cudaStream_t st) {
     if (!pp) return;
     Lists& L = pp->ls;
-    for (void* p : {(void*)L.l_row, (void*)L.l_s, (void*)L.l_cnt, (void*)L.l_key, (void*)L.b_row,
-                    (void*)L.b_s, (void*)L.b_e, (void*)L.m_row, (void*)L.m_s, (void*)L.m_e,
+    for (void* p : {(void*)L.u_row, (void*)L.u_s, (void*)L.u_cnt, (void*)L.m_row, (void*)L.m_s, (void*)L.m_e,
                     (void*)L.m_cnt, (void*)L.m_key, (void*)L.ctr})
         if (p) dfree(p, st);
     delete pp;

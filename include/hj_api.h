@@ -149,9 +149,11 @@ void* hj_context_stream(hj_context* ctx);
  * UnchainedHash::choose_directory_size, capped at 2^dir_cap_bits words),
  * "dir_cap_bits" (default 23: automatic directories of hj_execute stay within
  * 64 MB, cache resident; results do not depend on it), "radix_bits" (partition fan-out of the
- * build, 0..12), "probe_group" (threads per probe key in the write pass: 1, 4 (default), 8 or 32),
- * "light_max" (largest bucket scanned by one probe group before the bucket is
- * handed to a whole block), "timing" (1: record per-phase device times of
+ * build, 0..12), "probe_group" (output rows per thread of the match writer,
+ * so a probe key's matches spread over count / probe_group threads: 1, 2, 4,
+ * 8 (default), 16 or 32), "light_max" (a bucket of several keys with at most
+ * this many tuples is compared by the probing thread itself; larger ones by a
+ * warp or block per hit), "timing" (1: record per-phase device times of
  * each hj_execute, read with hj_result_phase_ms), "host_access" (1, default:
  * where the GPU can read and write pageable host memory, it moves input and
  * result pages itself; 0: host threads stage them through pinned memory),

@@ -121,6 +121,43 @@ def test_results_independent_of_tunables(engine, orc):
         assert np.array_equal(got[3], want[3]), opt
 
 
+def _irregular_int32(hj, vals, valid, rows_per_page):
+    """An INT32 column written in chunks of `rows_per_page` rows, so that its
+    pages are not the 1984-row dense pages read in place."""
+    pages = [hj.Column.int32(vals[i:i + rows_per_page], None if valid is None else valid[i:i + rows_per_page]).pages
+             for i in range(0, vals.size, rows_per_page)]
+    return hj.Column(hj.INT32, np.concatenate(pages))
+
+
+@pytest.mark.parametrize("form", ["pages", "plain", "tagged"])
+def test_probe_key_forms(engine, orc, hj, form):
+    """Probe keys staged in shared memory by bulk copies from each of their
+    device forms: dense pages read in place, decoded int32 (irregular pages
+    without NULLs) and value_t (with NULLs); tile ends at odd row counts and a
+    Zipf-heavy key whose bucket length saturates the summary."""
+    r = np.random.default_rng(17)
+    nb, npr = 120_001, 333_337
+    bkey = (r.zipf(1.3, nb) % 30_000).astype(np.int32)
+    bkey[:40_000] = 12345                     # a bucket far above the summary's length field
+    pkey = r.integers(-5, 32_000, npr).astype(np.int32)
+    pkey[::50_000] = 12345
+    pval = None if form != "tagged" else (r.random(npr) > 0.1).astype(np.uint8)
+    if form == "pages":
+        pcol = hj.Column.int32(pkey)
+    else:
+        pcol = _irregular_int32(hj, pkey, pval, 1001)
+    build = hj.Table(nb, [hj.Column.int32(bkey), hj.Column.int32(np.arange(nb, dtype=np.int32))])
+    probe = hj.Table(npr, [pcol, hj.Column.int32(np.arange(npr, dtype=np.int32))])
+    p = hj.Plan()
+    p.new_input(build)
+    p.new_input(probe)
+    p.new_scan_node(0, [(0, hj.INT32), (1, hj.INT32)])
+    p.new_scan_node(1, [(0, hj.INT32), (1, hj.INT32)])
+    p.root = p.new_join_node(True, 0, 1, 0, 0, [(0, hj.INT32), (1, hj.INT32), (3, hj.INT32)])
+    res = engine.execute(p)
+    assert_same(orc, res, orc.run(orc.port(), p), form)
+
+
 def test_resident_tables_give_the_same_result(engine, orc, hj):
     from hjgb300 import workloads
     w = workloads.c2(0.01)
