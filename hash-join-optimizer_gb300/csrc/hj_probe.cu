@@ -499,11 +499,17 @@ __global__ void __launch_bounds__(512)
 
 ProbeTab tab_of(const Table& t) { return ProbeTab{t.dir, t.summary, t.keys, t.rows, t.dir_bits}; }
 
+// How the count kernel reads a probe column's keys.  A bulk copy needs a
+// 16-byte aligned source; tiles start at multiples of 3968 rows (of 16-byte
+// multiples for every form), so the column's base address decides.  Columns
+// at other addresses (a caller's array at an arbitrary 4-byte offset) are
+// read by direct loads.
 int key_source(const KeyCol& pk) {
+    auto aligned = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; };
     if (pk.rid || pk.filt.n) return kSrcGather;
-    if (pk.col.tagged) return kSrcTagged;
-    if (pk.col.plain) return kSrcPlain;
-    return kSrcPages;
+    if (pk.col.tagged) return aligned(pk.col.tagged) ? kSrcTagged : kSrcGather;
+    if (pk.col.plain) return aligned(pk.col.plain) ? kSrcPlain : kSrcGather;
+    return aligned(pk.col.pages) ? kSrcPages : kSrcGather;
 }
 
 template <int SRC>

@@ -286,6 +286,19 @@ def test_table_probe_pairs(engine, hj, orc):
         assert np.array_equal(probe[pr], build[br])          # every pair is a match
         assert np.array_equal(np.bincount(pr, minlength=probe.size), want)  # and all are there
         assert np.unique(pr.astype(np.int64) << 32 | br).size == pr.size   # no duplicates
+        # keys at a 4-byte offset (no 16-byte alignment for the bulk copies):
+        # read by direct loads, same matches
+        ku = kp[1:]
+        want_u = orc.unchained_counts(build, probe[1:])
+        rc = L.hj_table_probe(engine.handle, t, ku.data_ptr(), None, ku.numel(), None, None, 0, C.byref(nm))
+        assert rc == hj.HJ_ERR_CAPACITY and nm.value == int(want_u.sum())
+        op = torch.empty(nm.value, dtype=torch.int32, device="cuda")
+        ob = torch.empty(nm.value, dtype=torch.int32, device="cuda")
+        assert L.hj_table_probe(engine.handle, t, ku.data_ptr(), None, ku.numel(), op.data_ptr(),
+                                ob.data_ptr(), nm.value, C.byref(nm)) == 0
+        pr, br = op.cpu().numpy(), ob.cpu().numpy()
+        assert np.array_equal(probe[1:][pr], build[br])
+        assert np.array_equal(np.bincount(pr, minlength=probe.size - 1), want_u)
     finally:
         L.hj_table_free(t)
 
