@@ -63,12 +63,10 @@ __global__ void __launch_bounds__(kThreads)
     const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
     for (uint64_t w0 = uint64_t(blockIdx.x) * blockDim.x + (threadIdx.x & ~31u); w0 < kc.n;
          w0 += stride) {
-        int32_t        key;
-        const bool     ok  = load_key(kc, w0 + (threadIdx.x & 31), key);
-        const unsigned act = __ballot_sync(0xffffffffu, ok);
+        int32_t    key;
+        const bool ok = load_key(kc, w0 + (threadIdx.x & 31), key);
         if (ok) {
-            // lanes of one partition add once (a Zipf-heavy key fills whole warps)
-            warp_agg_atomic_add(hist, uint32_t(bucket_of(fib_hash(key), R)), act);
+            atomicAdd(hist + uint32_t(bucket_of(fib_hash(key), R)), 1u);
             ++mine;
         }
     }
@@ -136,8 +134,7 @@ __global__ void __launch_bounds__(kST, 1024 / kST)
         const uint64_t i   = tile0 + uint64_t(k) * kST + threadIdx.x;
         const bool     ok  = load_key(kc, i, keys[k]);
         parts[k]           = ok ? uint32_t(bucket_of(fib_hash(keys[k]), R)) : 0;
-        const unsigned act = __ballot_sync(0xffffffffu, ok);
-        rank[k]            = ok ? warp_agg_atomic_add(off, parts[k], act) : 0;
+        rank[k]            = ok ? atomicAdd(off + parts[k], 1u) : 0;
         okmask |= uint32_t(ok) << k;
     }
     __syncthreads();

@@ -18,10 +18,12 @@
 //            of the bucket or none, decided by the first key; the hit is
 //            (probe row, bucket start, bucket length), the start read from the
 //            directory word for hits only;
-//   mixed    bucket of several keys: its tuples are compared, inline by the
-//            probing thread for buckets of at most light_max tuples, else by
-//            a warp or block per hit (k_mixed_count*).
-// Uniform hits are compacted with warp ballot/popc into shared memory and
+//   mixed    bucket of several keys: a bucket of at most min(light_max, 32)
+//            tuples is compared by the probing thread itself, which records
+//            the matching tuples as a 32-bit mask over the bucket and stages
+//            the hit with the uniform ones; larger buckets go to a list
+//            counted by a warp or block per hit (k_mixed_count*).
+// Staged hits are compacted with warp ballot/popc into shared memory and
 // flushed with ONE global atomic per 2048 rows (the reference's per-thread
 // work-stealing counter becomes this per-block reservation).
 //
@@ -68,7 +70,9 @@ struct ProbeTab {
 };
 
 struct Lists {
-    uint32_t *u_row, *u_s, *u_cnt;          // uniform hits: tuples [s, s + cnt) all match
+    // staged hits: tuples [s, s + cnt) all match when mask is 0, else the
+    // tuples s + i for the set bits i of mask (cnt = popcount)
+    uint32_t *u_row, *u_s, *u_cnt, *u_mask;
     uint32_t *m_row, *m_s, *m_e, *m_cnt;    // mixed hits: tuples [s, e) compared with m_key
     int32_t*  m_key;
     // 0 uniform hits, 1 mixed hits, 2 uniform matches, 3 mixed matches,
@@ -160,11 +164,12 @@ __global__ void __launch_bounds__(kPT)
     uint32_t*          s_row = reinterpret_cast<uint32_t*>(dyn + 2 * SB);     // kHalf each
     uint32_t*          s_s   = s_row + kHalf;
     uint32_t*          s_cnt = s_s + kHalf;
+    uint32_t*          s_msk = s_cnt + kHalf;
     __shared__ uint64_t bar[2];
     __shared__ uint32_t s_n, s_base, s_fail, s_cov;
     __shared__ unsigned long long s_red[33];
     const unsigned lane = threadIdx.x & 31;
-    uint64_t       tot_u = 0, tot_m = 0;
+    uint64_t       tot_u = 0;
     uint32_t       cov0 = 0, cov1 = 0;   // thread 0: rows each stage's copy covers
     uint32_t       iss0 = 0, iss1 = 0;   // thread 0: copies issued into each stage
     if (threadIdx.x == 0) {
@@ -217,7 +222,7 @@ __global__ void __launch_bounds__(kPT)
             // classify; the directory words (bucket start, and the end of a
             // saturated or mixed bucket) are loaded for hits only
             uint32_t s[kStep], e[kStep];
-            int      cls[kStep];  // 0 miss, 1 uniform, 2 mixed
+            int      cls[kStep];  // 0 miss, 1 uniform, 2 mixed (1 after an inline compare)
 #pragma unroll
             for (int it = 0; it < kStep; ++it) {
                 const uint64_t h = fib_hash(key[it]);
@@ -234,11 +239,20 @@ __global__ void __launch_bounds__(kPT)
                                                                          : s[it] + L;
                 }
             }
+            const uint32_t small = min(uint32_t(light_max), 32u);
 #pragma unroll
             for (int it = 0; it < kStep; ++it) {
                 const uint32_t i = base + uint32_t(it) * kPT + threadIdx.x;
                 const uint64_t j = r0 + i;
-                // uniform: staged in shared memory in lane order
+                // a small mixed bucket: compared here, its matches as a mask
+                uint32_t msk = 0, c = e[it] - s[it];
+                if (cls[it] == 2 && e[it] - s[it] <= small) {
+                    for (uint32_t q = 0; q < e[it] - s[it]; ++q)
+                        msk |= uint32_t(__ldg(T.keys + s[it] + q) == key[it]) << q;
+                    c       = __popc(msk);
+                    cls[it] = c ? 1 : 0;
+                }
+                // staged in shared memory in lane order
                 {
                     const unsigned bal = __ballot_sync(0xffffffffu, cls[it] == 1);
                     uint32_t       q0  = 0;
@@ -248,19 +262,14 @@ __global__ void __launch_bounds__(kPT)
                         const uint32_t q = q0 + __popc(bal & ((1u << lane) - 1));
                         s_row[q]         = uint32_t(j);
                         s_s[q]           = s[it];
-                        s_cnt[q]         = e[it] - s[it];
-                        tot_u += e[it] - s[it];
+                        s_cnt[q]         = c;
+                        s_msk[q]         = msk;
+                        tot_u += c;
                     }
                 }
-                // mixed: small buckets counted here, the rest later; rare, so
-                // warp-aggregated global atomics
-                uint32_t c = kUncounted;
-                if (cls[it] == 2 && e[it] - s[it] <= uint32_t(light_max)) {
-                    c = 0;
-                    for (uint32_t q = s[it]; q < e[it]; ++q) c += __ldg(T.keys + q) == key[it];
-                    if (c == 0) cls[it] = 0;
-                    tot_m += c;
-                }
+                // larger mixed buckets: counted later; rare, so warp-aggregated
+                // global atomics
+                c = kUncounted;
                 const unsigned bal = __ballot_sync(0xffffffffu, cls[it] == 2);
                 if (bal) {
                     unsigned long long q0 = 0;
@@ -283,9 +292,10 @@ __global__ void __launch_bounds__(kPT)
             __syncthreads();
             const uint32_t nst = s_n, gb = s_base;
             for (uint32_t q = threadIdx.x; q < nst; q += blockDim.x) {
-                Ls.u_row[gb + q] = s_row[q];
-                Ls.u_s[gb + q]   = s_s[q];
-                Ls.u_cnt[gb + q] = s_cnt[q];
+                Ls.u_row[gb + q]  = s_row[q];
+                Ls.u_s[gb + q]    = s_s[q];
+                Ls.u_cnt[gb + q]  = s_cnt[q];
+                Ls.u_mask[gb + q] = s_msk[q];
             }
             __syncthreads();
             if (threadIdx.x == 0) s_n = 0;
@@ -301,13 +311,9 @@ __global__ void __launch_bounds__(kPT)
             if (iss1) mbar_wait_bounded(&bar[1], (iss1 - 1) & 1, kWaitPolls);
         }
     }
-    unsigned long long t1, t2;
+    unsigned long long t1;
     block_exclusive_scan<unsigned long long>(tot_u, s_red, &t1);
-    block_exclusive_scan<unsigned long long>(tot_m, s_red, &t2);
-    if (threadIdx.x == 0) {
-        if (t1) atomicAdd(Ls.ctr + 2, t1);
-        if (t2) atomicAdd(Ls.ctr + 3, t2);
-    }
+    if (threadIdx.x == 0 && t1) atomicAdd(Ls.ctr + 2, t1);
 }
 
 // Mixed hits still uncounted: a warp each for buckets of up to kMixedWarpMax
@@ -372,11 +378,17 @@ __global__ void k_chunk_first(const uint64_t* __restrict__ off, uint64_t n_u, ui
     if (c < nchunks) chunk_first[c] = uint32_t(hit_of(off, n_u, c * chunk));
 }
 
-// Shared memory of k_write_uniform<G>: hit offsets, tuple bases and probe rows
-// of a chunk's hits (up to chunk + 1 each) plus one output stream's image.
-constexpr size_t write_uniform_smem(int G) { return (4 * (size_t(256) * G) + 4) * sizeof(uint32_t); }
-// (a chunk of CH outputs has at most CH + 1 hits: every hit holds at least one
-// output, plus the hit that starts at the next chunk's first position)
+// Shared memory of k_write_uniform<G>: one output stream's image, then the
+// chunk's hits (at most chunk + 1: every hit holds at least one output, plus
+// the hit that starts at the next chunk's first position): relative starts
+// (chunk + 2), probe rows, tuple starts, unclamped relative starts and masks.
+constexpr size_t write_uniform_smem(int G) { return (6 * (size_t(256) * G) + 6) * sizeof(uint32_t); }
+
+// Index of the k-th set bit of m (k < popcount(m)).
+__device__ __forceinline__ uint32_t nth_bit(uint32_t m, uint32_t k) {
+    for (uint32_t i = 0; i < k; ++i) m &= m - 1;
+    return uint32_t(__ffs(m) - 1);
+}
 
 template <int G>
 __global__ void __launch_bounds__(256)
@@ -384,10 +396,12 @@ __global__ void __launch_bounds__(256)
                     const uint32_t* __restrict__ chunk_first, uint64_t total, Outs outs) {
     constexpr uint32_t CH = 256u * G;
     extern __shared__ __align__(16) uint32_t wsh[];
-    uint32_t* s_rel = wsh;               // CH + 2: hit starts relative to the chunk, clamped to [0, len]
-    uint32_t* s_tb  = s_rel + CH + 2;    // CH + 1: tuple index of the chunk's position 0 within each hit
-    uint32_t* s_pr  = s_tb + CH + 1;     // CH + 1: probe row of each hit
-    uint32_t* s_val = s_pr + CH + 1;     // CH: one output stream (16-byte aligned: 3 CH + 4 words in)
+    uint32_t* s_val  = wsh;               // CH: one output stream
+    uint32_t* s_rel  = s_val + CH;        // CH + 2: hit starts relative to the chunk, clamped to [0, len]
+    uint32_t* s_pr   = s_rel + CH + 2;    // CH + 1: probe row of each hit
+    uint32_t* s_s    = s_pr + CH + 1;     // CH + 1: first tuple of each hit's bucket
+    uint32_t* s_orel = s_s + CH + 1;      // CH + 1: hit start - chunk start, mod 2^32
+    uint32_t* s_msk  = s_orel + CH + 1;   // CH + 1: match mask (0: every tuple)
     __shared__ uint64_t s_h[2];
     const uint64_t nchunks = (total + CH - 1) / CH;
     for (uint64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
@@ -405,8 +419,10 @@ __global__ void __launch_bounds__(256)
             const uint64_t rel = o > o0 ? o - o0 : 0;
             s_rel[q]           = uint32_t(umin64(rel, len));
             if (q < nh) {
-                s_pr[q] = __ldg(Ls.u_row + h0 + q);
-                s_tb[q] = __ldg(Ls.u_s + h0 + q) - uint32_t(o - o0);  // mod 2^32: start - (offset - o0)
+                s_pr[q]   = __ldg(Ls.u_row + h0 + q);
+                s_s[q]    = __ldg(Ls.u_s + h0 + q);
+                s_orel[q] = uint32_t(o - o0);
+                s_msk[q]  = __ldg(Ls.u_mask + h0 + q);
             }
         }
         __syncthreads();
@@ -425,8 +441,10 @@ __global__ void __launch_bounds__(256)
                 const uint32_t q = q0 + i;
                 if (q < len) {
                     while (s_rel[k + 1] <= q) ++k;
-                    prow[i] = s_pr[k];
-                    brow[i] = __ldg(T.rows + (s_tb[k] + q));
+                    const uint32_t idx = q - s_orel[k];  // match number within the hit
+                    const uint32_t m   = s_msk[k];
+                    prow[i]            = s_pr[k];
+                    brow[i]            = __ldg(T.rows + s_s[k] + (m ? nth_bit(m, idx) : idx));
                 }
             }
         }
@@ -515,7 +533,7 @@ int key_source(const KeyCol& pk) {
 template <int SRC>
 void launch_count_src(const ProbeTab& T, const KeyCol& pk, int light_max, const Lists& L, cudaStream_t st) {
     const uint64_t ntiles = (pk.n + kTileRows - 1) / kTileRows;
-    const size_t   smem   = 2 * size_t(stage_bytes(SRC)) + 3 * size_t(kHalf) * sizeof(uint32_t);
+    const size_t   smem   = 2 * size_t(stage_bytes(SRC)) + 4 * size_t(kHalf) * sizeof(uint32_t);
     HJ_CUDA(cudaFuncSetAttribute(k_probe_count<SRC>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     // resident blocks walk the tiles (each prefetching its next tile)
     int per_sm = 0;
@@ -545,8 +563,8 @@ int writer_items(int group) {
     case 1: return 1;
     case 2: return 2;
     case 4: return 4;
-    case 16: return 16;
-    case 32: return 32;
+    case 16:
+    case 32: return 16;  // 32 would take 196 KB of shared memory per block
     default: return 8;
     }
 }
@@ -571,7 +589,6 @@ void launch_uniform(int G, const ProbeTab& T, const Lists& L, uint64_t n_u, cons
     case 2: launch_uniform_g<2>(T, L, n_u, off, chunk_first, total, outs, st); break;
     case 4: launch_uniform_g<4>(T, L, n_u, off, chunk_first, total, outs, st); break;
     case 16: launch_uniform_g<16>(T, L, n_u, off, chunk_first, total, outs, st); break;
-    case 32: launch_uniform_g<32>(T, L, n_u, off, chunk_first, total, outs, st); break;
     default: launch_uniform_g<8>(T, L, n_u, off, chunk_first, total, outs, st); break;
     }
 }
@@ -613,6 +630,7 @@ uint64_t probe_count(const Table& t, const KeyCol& pk, const ProbeParams& prm, P
     L.u_row = dalloc_n<uint32_t>(n, st);
     L.u_s   = dalloc_n<uint32_t>(n, st);
     L.u_cnt = dalloc_n<uint32_t>(n, st);
+    L.u_mask = dalloc_n<uint32_t>(n, st);
     L.m_row = dalloc_n<uint32_t>(n, st);
     L.m_s   = dalloc_n<uint32_t>(n, st);
     L.m_e   = dalloc_n<uint32_t>(n, st);
@@ -682,7 +700,7 @@ struct Carve {
 
 size_t probe_scratch_bytes(uint64_t n) {
     const uint64_t tmp = scan_tmp_words(n) + 1;
-    return 256 + 8 * ((4 * n + 255) & ~uint64_t(255)) + 2 * ((8 * (n + 1) + 255) & ~uint64_t(255))
+    return 256 + 9 * ((4 * n + 255) & ~uint64_t(255)) + 2 * ((8 * (n + 1) + 255) & ~uint64_t(255))
          + ((8 * tmp + 255) & ~uint64_t(255));
 }
 
@@ -700,6 +718,7 @@ int probe_into_scratch(const Table& t, const KeyCol& pk, const ProbeParams& prm,
     L.u_row = c.take<uint32_t>(n);
     L.u_s   = c.take<uint32_t>(n);
     L.u_cnt = c.take<uint32_t>(n);
+    L.u_mask = c.take<uint32_t>(n);
     L.m_row = c.take<uint32_t>(n);
     L.m_s   = c.take<uint32_t>(n);
     L.m_e   = c.take<uint32_t>(n);
@@ -740,7 +759,7 @@ int probe_into_scratch(const Table& t, const KeyCol& pk, const ProbeParams& prm,
 void probe_free(ProbePlan* pp, cudaStream_t st) {
     if (!pp) return;
     Lists& L = pp->ls;
-    for (void* p : {(void*)L.u_row, (void*)L.u_s, (void*)L.u_cnt, (void*)L.m_row, (void*)L.m_s, (void*)L.m_e,
+    for (void* p : {(void*)L.u_row, (void*)L.u_s, (void*)L.u_cnt, (void*)L.u_mask, (void*)L.m_row, (void*)L.m_s, (void*)L.m_e,
                     (void*)L.m_cnt, (void*)L.m_key, (void*)L.ctr})
         if (p) dfree(p, st);
     delete pp;
