@@ -6,8 +6,8 @@
 // Bloom early-reject on the bucket's tag, then every tuple of the bucket with
 // an equal key is a match.
 //
-// Count pass (k_probe_count).  A block walks tiles of 3968 probe rows (two
-// dense INT32 pages).  The tile's keys are staged in shared memory by bulk
+// Count pass (k_probe_count).  A block walks tiles of 1984 probe rows (one
+// dense INT32 page).  The tile's keys are staged in shared memory by bulk
 // asynchronous copies (TMA) while the previous tile is probed: whole pages
 // for a dense column read in place, else the decoded int32 / value_t array.
 // Per key the probe issues ONE global load, the bucket's 8-byte summary
@@ -16,24 +16,26 @@
 //   miss     empty bucket, or the Bloom tag rejects the key;
 //   uniform  bucket of one key (mixed flag clear): the key matches every tuple
 //            of the bucket or none, decided by the first key; the hit is
-//            (probe row, bucket start, bucket length), the start read from the
-//            directory word for hits only;
+//            (probe row, bucket, length from the summary) -- no further load;
 //   mixed    bucket of several keys: a bucket of at most min(light_max, 32)
 //            tuples is compared by the probing thread itself, which records
 //            the matching tuples as a 32-bit mask over the bucket and stages
 //            the hit with the uniform ones; larger buckets go to a list
 //            counted by a warp or block per hit (k_mixed_count*).
-// Staged hits are compacted with warp ballot/popc into shared memory and
-// flushed with ONE global atomic per 2048 rows (the reference's per-thread
+// Staged hits are compacted with warp ballot/popc into shared memory.  Per
+// tile, ONE global 64-bit atomic reserves both the hits' list slots (high
+// word) and their output rows (low word), and a block scan of the staged
+// counts gives each hit its first output row, so list order and output order
+// agree and no device-wide prefix sum is needed (the reference's per-thread
 // work-stealing counter becomes this per-block reservation).
 //
-// Write pass.  A prefix sum of the uniform hits' lengths gives each hit its
-// first output slot.  k_write_uniform then walks the OUTPUT positions in
-// chunks of 256 x G (G outputs per thread, option probe_group): a chunk's
-// hits are located by the chunk map (k_chunk_first), each thread finds its
-// hit by binary search in shared memory and reads build rows rows[start + k]
-// consecutively, and every output row-id stream is written with coalesced
-// 16-byte stores through a shared-memory image.  Work is balanced by output
+// Write pass.  k_write_uniform walks the OUTPUT positions in chunks of
+// 256 x G (G outputs per thread, option probe_group): a chunk's hits are
+// located by the chunk map (k_chunk_first), a uniform hit's bucket start is
+// read from its directory word, each thread finds its hit by binary search in
+// shared memory and reads build rows rows[start + k] consecutively, and every
+// output row-id stream is written with coalesced stores through a
+// shared-memory image.  Work is balanced by output
 // rows, so one Zipf-heavy key with millions of tuples spreads over all SMs.
 // Mixed hits follow the uniform ones.  Every match writes one row id per
 // requested output stream, composed through the sides' row-id vectors (late
@@ -51,8 +53,9 @@ namespace {
 
 constexpr int      kPT        = 256;                    // threads of the count kernel
 constexpr int      kStep      = 8;                      // rows per thread in flight
-constexpr uint32_t kHalf      = uint32_t(kPT) * kStep;  // rows per staging flush (2048)
-constexpr uint32_t kTileRows  = 2 * uint32_t(kDenseRows);  // 3968 rows per staged tile
+constexpr uint32_t kTileRows  = uint32_t(kDenseRows);   // 1984 rows per staged tile (one page)
+static_assert(kTileRows <= uint32_t(kPT) * kStep, "a tile is one pass of the count kernel");
+static_assert(kPT * kStep == 2048 && kPT == 256, "the staged-hit scan covers 8 warps x 8 rows of 32");
 constexpr uint32_t kUncounted = 0xffffffffu;            // mixed hit still to be counted
 constexpr uint32_t kMixedWarpMax = 4096;                // mixed buckets up to this size: one warp each
 constexpr uint32_t kWaitPolls    = 1u << 20;            // bound of a staging wait (mbarrier polls)
@@ -70,13 +73,14 @@ struct ProbeTab {
 };
 
 struct Lists {
-    // staged hits: tuples [s, s + cnt) all match when mask is 0, else the
-    // tuples s + i for the set bits i of mask (cnt = popcount)
-    uint32_t *u_row, *u_s, *u_cnt, *u_mask;
+    // staged hits, in output order: hit h owns output rows [off[h], off[h + 1])
+    // (the last up to the staged total); mask 0: the whole bucket sp matches,
+    // else the tuples sp + i for the set bits i of mask
+    uint32_t *u_row, *u_sp, *u_off, *u_mask;
     uint32_t *m_row, *m_s, *m_e, *m_cnt;    // mixed hits: tuples [s, e) compared with m_key
     int32_t*  m_key;
-    // 0 uniform hits, 1 mixed hits, 2 uniform matches, 3 mixed matches,
-    // 4 staging waits that gave up (an error)
+    // 0 staged hits << 32 | staged matches mod 2^32, 1 mixed hits, 2 staged
+    // matches, 3 mixed matches, 4 staging waits that gave up (an error)
     unsigned long long* ctr;
 };
 
@@ -96,7 +100,7 @@ __device__ __forceinline__ void emit(const Outs& outs, uint64_t pos, uint32_t pr
 
 // Bytes of one staged tile of each key source (0: no staging).
 __host__ __device__ constexpr uint32_t stage_bytes(int src) {
-    return src == kSrcPages    ? 2u * kPage
+    return src == kSrcPages    ? uint32_t(kPage)
          : src == kSrcPlain    ? kTileRows * 4u
          : src == kSrcTagged   ? kTileRows * 8u
                                : 0u;
@@ -111,10 +115,8 @@ __device__ __forceinline__ uint32_t stage_tile(const KeyCol& pk, uint64_t tile, 
     uint32_t       bytes = 0, covered = 0;
     const void*    src   = nullptr;
     if (SRC == kSrcPages) {
-        const uint64_t npages = (pk.n + kDenseRows - 1) / kDenseRows;
-        const uint64_t p0     = r0 / kDenseRows;
-        bytes   = uint32_t(umin64(2, npages - p0)) * kPage;
-        src     = pk.col.pages + p0 * kPage;
+        bytes   = kPage;
+        src     = pk.col.pages + tile * kPage;
         covered = nrows;
     } else if (SRC == kSrcPlain) {
         covered = nrows & ~3u;
@@ -136,8 +138,7 @@ template <int SRC>
 __device__ __forceinline__ bool tile_key(const KeyCol& pk, const uint8_t* stage, uint32_t covered, uint32_t i,
                                          uint64_t r, int32_t& key) {
     if (SRC == kSrcPages) {
-        const uint32_t pl = i / kDenseRows;
-        key = reinterpret_cast<const int32_t*>(stage + size_t(pl) * kPage + 4)[i - pl * kDenseRows];
+        key = reinterpret_cast<const int32_t*>(stage + 4)[i];
         return true;
     } else if (SRC == kSrcPlain) {
         key = i < covered ? reinterpret_cast<const int32_t*>(stage)[i] : __ldg(pk.col.plain + r);
@@ -159,21 +160,21 @@ template <int SRC>
 __global__ void __launch_bounds__(kPT)
     k_probe_count(ProbeTab T, KeyCol pk, int light_max, Lists Ls, uint64_t ntiles) {
     extern __shared__ __align__(128) uint8_t dyn[];
-    constexpr uint32_t SB   = stage_bytes(SRC);
-    uint8_t*           stg  = dyn;                                            // 2 stages
-    uint32_t*          s_row = reinterpret_cast<uint32_t*>(dyn + 2 * SB);     // kHalf each
-    uint32_t*          s_s   = s_row + kHalf;
-    uint32_t*          s_cnt = s_s + kHalf;
-    uint32_t*          s_msk = s_cnt + kHalf;
+    constexpr uint32_t SB    = stage_bytes(SRC);
+    constexpr uint32_t kCap  = uint32_t(kPT) * kStep;                       // staged hits per tile
+    uint8_t*           stg   = dyn;                                          // 2 stages
+    uint32_t*          s_row = reinterpret_cast<uint32_t*>(dyn + 2 * SB);    // kCap each
+    uint32_t*          s_sp  = s_row + kCap;
+    uint32_t*          s_cnt = s_sp + kCap;
+    uint32_t*          s_msk = s_cnt + kCap;
     __shared__ uint64_t bar[2];
-    __shared__ uint32_t s_n, s_base, s_fail, s_cov;
-    __shared__ unsigned long long s_red[33];
+    __shared__ uint32_t s_n, s_fail, s_cov;
+    __shared__ unsigned long long s_base, s_red[33];
     const unsigned lane = threadIdx.x & 31;
-    uint64_t       tot_u = 0;
     uint32_t       cov0 = 0, cov1 = 0;   // thread 0: rows each stage's copy covers
     uint32_t       iss0 = 0, iss1 = 0;   // thread 0: copies issued into each stage
     if (threadIdx.x == 0) {
-        s_n = 0;
+        s_n    = 0;
         s_fail = 0;
         if (SRC != kSrcGather) {
             mbar_init(&bar[0]);
@@ -185,7 +186,8 @@ __global__ void __launch_bounds__(kPT)
         cov0 = stage_tile<SRC>(pk, blockIdx.x, stg, &bar[0]);
         iss0 = 1;
     }
-    uint32_t k = 0;
+    const uint32_t small = min(uint32_t(light_max), 32u);
+    uint32_t       k     = 0;
     for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++k) {
         const uint32_t st = k & 1;
         if (SRC != kSrcGather) {
@@ -206,101 +208,125 @@ __global__ void __launch_bounds__(kPT)
         const uint64_t r0    = tile * kTileRows;
         const uint32_t nrows = uint32_t(umin64(kTileRows, pk.n - r0));
         const uint8_t* stage = stg + st * SB;
-        for (uint32_t base = 0; base < nrows; base += kHalf) {
-            int32_t  key[kStep];
-            bool     ok[kStep];
-            uint64_t w[kStep];
+        int32_t  key[kStep];
+        bool     ok[kStep];
+        uint64_t w[kStep];
 #pragma unroll
-            for (int it = 0; it < kStep; ++it) {
-                const uint32_t i = base + uint32_t(it) * kPT + threadIdx.x;
-                ok[it]           = false;
-                key[it]          = 0;
-                w[it]            = 0;
-                if (i < nrows) ok[it] = tile_key<SRC>(pk, stage, cov, i, r0 + i, key[it]);
-                if (ok[it]) w[it] = __ldg(T.sum + bucket_of(fib_hash(key[it]), T.b));
-            }
-            // classify; the directory words (bucket start, and the end of a
-            // saturated or mixed bucket) are loaded for hits only
-            uint32_t s[kStep], e[kStep];
-            int      cls[kStep];  // 0 miss, 1 uniform, 2 mixed (1 after an inline compare)
-#pragma unroll
-            for (int it = 0; it < kStep; ++it) {
-                const uint64_t h = fib_hash(key[it]);
-                const uint32_t m = bloom_mask(h);
-                const uint32_t L = sum_len(w[it]);
-                cls[it]          = 0;
-                if (ok[it] && L != 0 && (sum_bloom(w[it]) & m) == m)
-                    cls[it] = sum_mixed(w[it]) ? 2 : (sum_head(w[it]) == key[it] ? 1 : 0);
-                s[it] = e[it] = 0;
-                if (cls[it]) {
-                    const uint64_t p = bucket_of(h, T.b);
-                    s[it]            = uint32_t(__ldg(T.dir + p) >> 16);
-                    e[it]            = (cls[it] == 2 || L == kSumLenMax) ? uint32_t(__ldg(T.dir + p + 1) >> 16)
-                                                                         : s[it] + L;
-                }
-            }
-            const uint32_t small = min(uint32_t(light_max), 32u);
-#pragma unroll
-            for (int it = 0; it < kStep; ++it) {
-                const uint32_t i = base + uint32_t(it) * kPT + threadIdx.x;
-                const uint64_t j = r0 + i;
-                // a small mixed bucket: compared here, its matches as a mask
-                uint32_t msk = 0, c = e[it] - s[it];
-                if (cls[it] == 2 && e[it] - s[it] <= small) {
-                    for (uint32_t q = 0; q < e[it] - s[it]; ++q)
-                        msk |= uint32_t(__ldg(T.keys + s[it] + q) == key[it]) << q;
-                    c       = __popc(msk);
-                    cls[it] = c ? 1 : 0;
-                }
-                // staged in shared memory in lane order
-                {
-                    const unsigned bal = __ballot_sync(0xffffffffu, cls[it] == 1);
-                    uint32_t       q0  = 0;
-                    if (lane == 0 && bal) q0 = atomicAdd(&s_n, uint32_t(__popc(bal)));
-                    q0 = __shfl_sync(0xffffffffu, q0, 0);
-                    if (cls[it] == 1) {
-                        const uint32_t q = q0 + __popc(bal & ((1u << lane) - 1));
-                        s_row[q]         = uint32_t(j);
-                        s_s[q]           = s[it];
-                        s_cnt[q]         = c;
-                        s_msk[q]         = msk;
-                        tot_u += c;
-                    }
-                }
-                // larger mixed buckets: counted later; rare, so warp-aggregated
-                // global atomics
-                c = kUncounted;
-                const unsigned bal = __ballot_sync(0xffffffffu, cls[it] == 2);
-                if (bal) {
-                    unsigned long long q0 = 0;
-                    if (lane == 0) q0 = atomicAdd(Ls.ctr + 1, (unsigned long long)__popc(bal));
-                    q0 = __shfl_sync(0xffffffffu, q0, 0);
-                    if (cls[it] == 2) {
-                        const uint64_t q = q0 + __popc(bal & ((1u << lane) - 1));
-                        Ls.m_row[q]      = uint32_t(j);
-                        Ls.m_s[q]        = s[it];
-                        Ls.m_e[q]        = e[it];
-                        Ls.m_key[q]      = key[it];
-                        Ls.m_cnt[q]      = c;
-                    }
-                }
-            }
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                s_base = s_n ? uint32_t(atomicAdd(Ls.ctr + 0, (unsigned long long)s_n)) : 0u;
-            }
-            __syncthreads();
-            const uint32_t nst = s_n, gb = s_base;
-            for (uint32_t q = threadIdx.x; q < nst; q += blockDim.x) {
-                Ls.u_row[gb + q]  = s_row[q];
-                Ls.u_s[gb + q]    = s_s[q];
-                Ls.u_cnt[gb + q]  = s_cnt[q];
-                Ls.u_mask[gb + q] = s_msk[q];
-            }
-            __syncthreads();
-            if (threadIdx.x == 0) s_n = 0;
-            __syncthreads();
+        for (int it = 0; it < kStep; ++it) {
+            const uint32_t i = uint32_t(it) * kPT + threadIdx.x;
+            ok[it]           = false;
+            key[it]          = 0;
+            w[it]            = 0;
+            if (i < nrows) ok[it] = tile_key<SRC>(pk, stage, cov, i, r0 + i, key[it]);
+            if (ok[it]) w[it] = __ldg(T.sum + bucket_of(fib_hash(key[it]), T.b));
         }
+        // classify: 0 miss, 1 uniform, 2 mixed.  Directory words are read only
+        // for mixed buckets and for uniform buckets whose length saturated
+        // the summary's field
+        uint32_t s[kStep], e[kStep], L[kStep];
+        int      cls[kStep];
+#pragma unroll
+        for (int it = 0; it < kStep; ++it) {
+            const uint64_t h = fib_hash(key[it]);
+            const uint32_t m = bloom_mask(h);
+            L[it]            = sum_len(w[it]);
+            cls[it]          = 0;
+            if (ok[it] && L[it] != 0 && (sum_bloom(w[it]) & m) == m)
+                cls[it] = sum_mixed(w[it]) ? 2 : (sum_head(w[it]) == key[it] ? 1 : 0);
+            const uint64_t p = bucket_of(h, T.b);
+            s[it]            = uint32_t(p);
+            e[it]            = 0;
+            if (cls[it] == 2 || (cls[it] == 1 && L[it] == kSumLenMax)) {
+                const uint32_t b0 = uint32_t(__ldg(T.dir + p) >> 16);
+                L[it]             = uint32_t(__ldg(T.dir + p + 1) >> 16) - b0;
+                if (cls[it] == 2) s[it] = b0;
+                e[it] = b0 + L[it];
+            }
+        }
+#pragma unroll
+        for (int it = 0; it < kStep; ++it) {
+            const uint32_t i = uint32_t(it) * kPT + threadIdx.x;
+            const uint64_t j = r0 + i;
+            // a small mixed bucket: compared here, its matches as a mask
+            uint32_t msk = 0, c = L[it];
+            if (cls[it] == 2 && L[it] <= small) {
+                for (uint32_t q = 0; q < L[it]; ++q) msk |= uint32_t(__ldg(T.keys + s[it] + q) == key[it]) << q;
+                c       = __popc(msk);
+                cls[it] = c ? 1 : 0;
+            }
+            // staged in shared memory in lane order: (row, bucket or first
+            // tuple, count, mask)
+            {
+                const unsigned bal = __ballot_sync(0xffffffffu, cls[it] == 1);
+                uint32_t       q0  = 0;
+                if (lane == 0 && bal) q0 = atomicAdd(&s_n, uint32_t(__popc(bal)));
+                q0 = __shfl_sync(0xffffffffu, q0, 0);
+                if (cls[it] == 1) {
+                    const uint32_t q = q0 + __popc(bal & ((1u << lane) - 1));
+                    s_row[q]         = uint32_t(j);
+                    s_sp[q]          = s[it];
+                    s_cnt[q]         = c;
+                    s_msk[q]         = msk;
+                }
+            }
+            // larger mixed buckets: counted later; rare, so warp-aggregated
+            // global atomics
+            const unsigned bal = __ballot_sync(0xffffffffu, cls[it] == 2);
+            if (bal) {
+                unsigned long long q0 = 0;
+                if (lane == 0) q0 = atomicAdd(Ls.ctr + 1, (unsigned long long)__popc(bal));
+                q0 = __shfl_sync(0xffffffffu, q0, 0);
+                if (cls[it] == 2) {
+                    const uint64_t q = q0 + __popc(bal & ((1u << lane) - 1));
+                    Ls.m_row[q]      = uint32_t(j);
+                    Ls.m_s[q]        = s[it];
+                    Ls.m_e[q]        = e[it];
+                    Ls.m_key[q]      = key[it];
+                    Ls.m_cnt[q]      = kUncounted;
+                }
+            }
+        }
+        __syncthreads();
+        // output rows of the staged hits: exclusive prefix of their counts in
+        // staging order.  Warp w scans entries 256 w .. 256 w + 255 in rows of
+        // 32 (lane i reads entry 32 q + i: no bank conflicts), leaving each
+        // entry's prefix within its warp in s_cnt; then the warps' totals.
+        const uint32_t nst  = s_n;
+        const uint32_t warp = threadIdx.x >> 5;
+        uint64_t       wsum = 0;
+#pragma unroll
+        for (int q = 0; q < kStep; ++q) {
+            const uint32_t x   = (warp * kStep + q) * 32 + lane;
+            const uint32_t c   = x < nst ? s_cnt[x] : 0u;
+            const uint64_t inc = warp_inclusive_scan<uint64_t>(c);
+            if (x < nst) s_cnt[x] = uint32_t(wsum + inc - c);
+            wsum += __shfl_sync(0xffffffffu, inc, 31);
+        }
+        if (lane == 0) s_red[warp] = wsum;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned long long tile_sum = 0;
+            for (int w = 0; w < kPT / 32; ++w) {
+                const unsigned long long x = s_red[w];
+                s_red[w]                   = tile_sum;  // warp bases
+                tile_sum += x;
+            }
+            // one reservation: list slots in the high word, output rows in the
+            // low word (mod 2^32; the exact total is summed beside it)
+            s_base = nst ? atomicAdd(Ls.ctr + 0, (uint64_t(nst) << 32) + (tile_sum & 0xffffffffull)) : 0ull;
+            if (tile_sum) atomicAdd(Ls.ctr + 2, tile_sum);
+        }
+        __syncthreads();
+        const uint32_t hb = uint32_t(s_base >> 32), ob = uint32_t(s_base);
+        for (uint32_t x = threadIdx.x; x < nst; x += blockDim.x) {
+            Ls.u_row[hb + x]  = s_row[x];
+            Ls.u_sp[hb + x]   = s_sp[x];
+            Ls.u_off[hb + x]  = ob + uint32_t(s_red[x >> 8]) + s_cnt[x];
+            Ls.u_mask[hb + x] = s_msk[x];
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) s_n = 0;
+        __syncthreads();
     }
     if (SRC != kSrcGather) {
         // a block that gave up waits (bounded) for the copies it issued, so no
@@ -311,9 +337,6 @@ __global__ void __launch_bounds__(kPT)
             if (iss1) mbar_wait_bounded(&bar[1], (iss1 - 1) & 1, kWaitPolls);
         }
     }
-    unsigned long long t1;
-    block_exclusive_scan<unsigned long long>(tot_u, s_red, &t1);
-    if (threadIdx.x == 0 && t1) atomicAdd(Ls.ctr + 2, t1);
 }
 
 // Mixed hits still uncounted: a warp each for buckets of up to kMixedWarpMax
@@ -361,7 +384,7 @@ __global__ void __launch_bounds__(512) k_mixed_count(ProbeTab T, Lists Ls) {
 }
 
 // Largest h < n with off[h] <= x (off non-decreasing, off[0] = 0).
-__device__ __forceinline__ uint64_t hit_of(const uint64_t* __restrict__ off, uint64_t n, uint64_t x) {
+__device__ __forceinline__ uint64_t hit_of(const uint32_t* __restrict__ off, uint64_t n, uint64_t x) {
     uint64_t lo = 0, hi = n;
     while (hi - lo > 1) {
         const uint64_t mid = (lo + hi) >> 1;
@@ -372,7 +395,7 @@ __device__ __forceinline__ uint64_t hit_of(const uint64_t* __restrict__ off, uin
 }
 
 // chunk_first[c] = the uniform hit holding output position c * chunk.
-__global__ void k_chunk_first(const uint64_t* __restrict__ off, uint64_t n_u, uint64_t nchunks, uint32_t chunk,
+__global__ void k_chunk_first(const uint32_t* __restrict__ off, uint64_t n_u, uint64_t nchunks, uint32_t chunk,
                               uint32_t* __restrict__ chunk_first) {
     const uint64_t c = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (c < nchunks) chunk_first[c] = uint32_t(hit_of(off, n_u, c * chunk));
@@ -392,8 +415,9 @@ __device__ __forceinline__ uint32_t nth_bit(uint32_t m, uint32_t k) {
 
 template <int G>
 __global__ void __launch_bounds__(256)
-    k_write_uniform(ProbeTab T, Lists Ls, uint64_t n_u, const uint64_t* __restrict__ off,
-                    const uint32_t* __restrict__ chunk_first, uint64_t total, Outs outs) {
+    k_write_uniform(ProbeTab T, Lists Ls, uint64_t n_u, const uint32_t* __restrict__ chunk_first, uint64_t total,
+                    Outs outs) {
+    const uint32_t* __restrict__ off = Ls.u_off;
     constexpr uint32_t CH = 256u * G;
     extern __shared__ __align__(16) uint32_t wsh[];
     uint32_t* s_val  = wsh;               // CH: one output stream
@@ -415,14 +439,18 @@ __global__ void __launch_bounds__(256)
         const uint64_t h0 = s_h[0];
         const uint32_t nh = uint32_t(s_h[1] - h0) + 1;  // hits h0 .. h0 + nh - 1 cover the chunk
         for (uint32_t q = threadIdx.x; q <= nh; q += blockDim.x) {
-            const uint64_t o   = __ldg(off + h0 + q);
+            const uint64_t hq  = h0 + q;
+            const uint64_t o   = hq < n_u ? uint64_t(__ldg(off + hq)) : total;
             const uint64_t rel = o > o0 ? o - o0 : 0;
             s_rel[q]           = uint32_t(umin64(rel, len));
             if (q < nh) {
-                s_pr[q]   = __ldg(Ls.u_row + h0 + q);
-                s_s[q]    = __ldg(Ls.u_s + h0 + q);
+                const uint32_t m  = __ldg(Ls.u_mask + hq);
+                const uint32_t sp = __ldg(Ls.u_sp + hq);
+                s_pr[q]   = __ldg(Ls.u_row + hq);
+                // a uniform hit names its bucket: the start is its directory word's
+                s_s[q]    = m ? sp : uint32_t(__ldg(T.dir + sp) >> 16);
                 s_orel[q] = uint32_t(o - o0);
-                s_msk[q]  = __ldg(Ls.u_mask + h0 + q);
+                s_msk[q]  = m;
             }
         }
         __syncthreads();
@@ -533,7 +561,7 @@ int key_source(const KeyCol& pk) {
 template <int SRC>
 void launch_count_src(const ProbeTab& T, const KeyCol& pk, int light_max, const Lists& L, cudaStream_t st) {
     const uint64_t ntiles = (pk.n + kTileRows - 1) / kTileRows;
-    const size_t   smem   = 2 * size_t(stage_bytes(SRC)) + 4 * size_t(kHalf) * sizeof(uint32_t);
+    const size_t   smem   = 2 * size_t(stage_bytes(SRC)) + 4 * size_t(kPT) * kStep * sizeof(uint32_t);
     HJ_CUDA(cudaFuncSetAttribute(k_probe_count<SRC>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     // resident blocks walk the tiles (each prefetching its next tile)
     int per_sm = 0;
@@ -570,26 +598,28 @@ int writer_items(int group) {
 }
 
 template <int G>
-void launch_uniform_g(const ProbeTab& T, const Lists& L, uint64_t n_u, const uint64_t* off, const uint32_t* chunk_first,
-                      uint64_t total, const Outs& outs, cudaStream_t st) {
+void launch_uniform_g(const ProbeTab& T, const Lists& L, uint64_t n_u, const uint32_t* chunk_first, uint64_t total,
+                      const Outs& outs, cudaStream_t st) {
     const size_t smem = write_uniform_smem(G);
     HJ_CUDA(cudaFuncSetAttribute(k_write_uniform<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     int per_sm = 0;
     HJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_write_uniform<G>, 256, smem));
     const uint64_t nchunks = (total + 256u * G - 1) / (256u * G);
     const uint64_t grid    = std::max<uint64_t>(1, std::min<uint64_t>(nchunks, uint64_t(num_sms()) * std::max(1, per_sm)));
-    k_write_uniform<G><<<unsigned(grid), 256, smem, st>>>(T, L, n_u, off, chunk_first, total, outs);
+    k_write_uniform<G><<<unsigned(grid), 256, smem, st>>>(T, L, n_u, chunk_first, total, outs);
     HJ_LAUNCH_CHECK();
 }
 
-void launch_uniform(int G, const ProbeTab& T, const Lists& L, uint64_t n_u, const uint64_t* off,
-                    const uint32_t* chunk_first, uint64_t total, const Outs& outs, cudaStream_t st) {
+// The staged hits' matches (total of them, < 2^32) into the output streams.
+void launch_uniform(int G, const ProbeTab& T, const Lists& L, uint64_t n_u, const uint32_t* chunk_first,
+                    uint64_t total, const Outs& outs, cudaStream_t st) {
+    if (total > 0xffffffffull) throw Error(HJ_ERR_INVALID, "join result exceeds 2^32 rows");
     switch (G) {
-    case 1: launch_uniform_g<1>(T, L, n_u, off, chunk_first, total, outs, st); break;
-    case 2: launch_uniform_g<2>(T, L, n_u, off, chunk_first, total, outs, st); break;
-    case 4: launch_uniform_g<4>(T, L, n_u, off, chunk_first, total, outs, st); break;
-    case 16: launch_uniform_g<16>(T, L, n_u, off, chunk_first, total, outs, st); break;
-    default: launch_uniform_g<8>(T, L, n_u, off, chunk_first, total, outs, st); break;
+    case 1: launch_uniform_g<1>(T, L, n_u, chunk_first, total, outs, st); break;
+    case 2: launch_uniform_g<2>(T, L, n_u, chunk_first, total, outs, st); break;
+    case 4: launch_uniform_g<4>(T, L, n_u, chunk_first, total, outs, st); break;
+    case 16: launch_uniform_g<16>(T, L, n_u, chunk_first, total, outs, st); break;
+    default: launch_uniform_g<8>(T, L, n_u, chunk_first, total, outs, st); break;
     }
 }
 
@@ -628,8 +658,8 @@ uint64_t probe_count(const Table& t, const KeyCol& pk, const ProbeParams& prm, P
     pp->cap          = n;
     Lists& L         = pp->ls;
     L.u_row = dalloc_n<uint32_t>(n, st);
-    L.u_s   = dalloc_n<uint32_t>(n, st);
-    L.u_cnt = dalloc_n<uint32_t>(n, st);
+    L.u_sp  = dalloc_n<uint32_t>(n, st);
+    L.u_off = dalloc_n<uint32_t>(n, st);
     L.u_mask = dalloc_n<uint32_t>(n, st);
     L.m_row = dalloc_n<uint32_t>(n, st);
     L.m_s   = dalloc_n<uint32_t>(n, st);
@@ -644,7 +674,7 @@ uint64_t probe_count(const Table& t, const KeyCol& pk, const ProbeParams& prm, P
     readback(pp->host, L.ctr, 5 * sizeof(uint64_t), true, st);  // page-locked scratch
     HJ_CUDA(cudaStreamSynchronize(st));
     check_staging(pp->host);
-    pp->n_u   = pp->host[0];
+    pp->n_u   = pp->host[0] >> 32;
     pp->n_m   = pp->host[1];
     pp->tot_u = pp->host[2];
     pp->tot_m = pp->host[3];
@@ -665,13 +695,10 @@ void probe_write(const Table& t, const KeyCol& pk, ProbePlan* pp, const RidOut* 
         const int      G       = writer_items(pp->group);
         const uint64_t chunk   = 256u * uint64_t(G);
         const uint64_t nchunks = (pp->tot_u + chunk - 1) / chunk;
-        uint64_t*      off     = dalloc_n<uint64_t>(pp->n_u + 1, st);
         uint32_t*      cfirst  = dalloc_n<uint32_t>(nchunks + 1, st);
-        scan_exclusive_u32_to_u64(L.u_cnt, off, pp->n_u, st);
-        k_chunk_first<<<div_up(nchunks, 256), 256, 0, st>>>(off, pp->n_u, nchunks, uint32_t(chunk), cfirst);
+        k_chunk_first<<<div_up(nchunks, 256), 256, 0, st>>>(L.u_off, pp->n_u, nchunks, uint32_t(chunk), cfirst);
         HJ_LAUNCH_CHECK();
-        launch_uniform(G, T, L, pp->n_u, off, cfirst, pp->tot_u, outs, st);
-        dfree(off, st);
+        launch_uniform(G, T, L, pp->n_u, cfirst, pp->tot_u, outs, st);
         dfree(cfirst, st);
     }
     if (pp->n_m) {
@@ -700,7 +727,7 @@ struct Carve {
 
 size_t probe_scratch_bytes(uint64_t n) {
     const uint64_t tmp = scan_tmp_words(n) + 1;
-    return 256 + 9 * ((4 * n + 255) & ~uint64_t(255)) + 2 * ((8 * (n + 1) + 255) & ~uint64_t(255))
+    return 256 + 9 * ((4 * n + 255) & ~uint64_t(255)) + ((8 * (n + 1) + 255) & ~uint64_t(255))
          + ((8 * tmp + 255) & ~uint64_t(255));
 }
 
@@ -712,19 +739,18 @@ int probe_into_scratch(const Table& t, const KeyCol& pk, const ProbeParams& prm,
     const uint64_t n = pk.n;
     if (probe_scratch_bytes(n) > scratch_bytes) throw Error(HJ_ERR_INVALID, "probe scratch too small");
     Lists     L{};
-    uint64_t *u_off, *m_off, *tmp;
+    uint64_t *m_off, *tmp;
     Carve     c{scratch};
     L.ctr   = c.take<unsigned long long>(8);
     L.u_row = c.take<uint32_t>(n);
-    L.u_s   = c.take<uint32_t>(n);
-    L.u_cnt = c.take<uint32_t>(n);
+    L.u_sp  = c.take<uint32_t>(n);
+    L.u_off = c.take<uint32_t>(n);
     L.u_mask = c.take<uint32_t>(n);
     L.m_row = c.take<uint32_t>(n);
     L.m_s   = c.take<uint32_t>(n);
     L.m_e   = c.take<uint32_t>(n);
     L.m_cnt = c.take<uint32_t>(n);
     L.m_key = c.take<int32_t>(n);
-    u_off   = c.take<uint64_t>(n + 1);
     m_off   = c.take<uint64_t>(n + 1);
     tmp     = c.take<uint64_t>(scan_tmp_words(n) + 1);
     // the scratch keeps the previous call's contents: the counters restart at zero
@@ -735,7 +761,7 @@ int probe_into_scratch(const Table& t, const KeyCol& pk, const ProbeParams& prm,
     readback(h, L.ctr, 5 * sizeof(uint64_t), true, st);  // page-locked scratch
     HJ_CUDA(cudaStreamSynchronize(st));
     check_staging(h);
-    const uint64_t n_u = h[0], n_m = h[1], tot_u = h[2], total = h[2] + h[3];
+    const uint64_t n_u = h[0] >> 32, n_m = h[1], tot_u = h[2], total = h[2] + h[3];
     *num_matches = total;
     if (total > capacity) return HJ_ERR_CAPACITY;
     if (total == 0) return HJ_OK;
@@ -744,10 +770,9 @@ int probe_into_scratch(const Table& t, const KeyCol& pk, const ProbeParams& prm,
     outs.o[0] = RidOut{0, nullptr, out_probe};
     outs.o[1] = RidOut{1, nullptr, out_build};
     if (n_u) {
-        scan_exclusive_u32_to_u64_into(L.u_cnt, u_off, n_u, tmp, st);
         // no chunk map (its size would follow the match count): each chunk
         // finds its first hit by binary search
-        launch_uniform(writer_items(prm.group), T, L, n_u, u_off, nullptr, tot_u, outs, st);
+        launch_uniform(writer_items(prm.group), T, L, n_u, nullptr, tot_u, outs, st);
     }
     if (n_m) {
         scan_exclusive_u32_to_u64_into(L.m_cnt, m_off, n_m, tmp, st);
@@ -759,7 +784,7 @@ int probe_into_scratch(const Table& t, const KeyCol& pk, const ProbeParams& prm,
 void probe_free(ProbePlan* pp, cudaStream_t st) {
     if (!pp) return;
     Lists& L = pp->ls;
-    for (void* p : {(void*)L.u_row, (void*)L.u_s, (void*)L.u_cnt, (void*)L.u_mask, (void*)L.m_row, (void*)L.m_s, (void*)L.m_e,
+    for (void* p : {(void*)L.u_row, (void*)L.u_sp, (void*)L.u_off, (void*)L.u_mask, (void*)L.m_row, (void*)L.m_s, (void*)L.m_e,
                     (void*)L.m_cnt, (void*)L.m_key, (void*)L.ctr})
         if (p) dfree(p, st);
     delete pp;
