@@ -59,15 +59,20 @@ __global__ void __launch_bounds__(kThreads)
     const uint32_t P = 1u << R;
     for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) hist[i] = 0;
     __syncthreads();
-    uint32_t       mine   = 0;
-    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
-    for (uint64_t w0 = uint64_t(blockIdx.x) * blockDim.x + (threadIdx.x & ~31u); w0 < kc.n;
-         w0 += stride) {
-        int32_t    key;
-        const bool ok = load_key(kc, w0 + (threadIdx.x & 31), key);
-        if (ok) {
-            atomicAdd(hist + uint32_t(bucket_of(fib_hash(key), R)), 1u);
-            ++mine;
+    uint32_t       mine = 0;
+    constexpr int  kU   = 8;  // keys per thread loaded before any of them is counted
+    const uint64_t step = uint64_t(gridDim.x) * blockDim.x * kU;
+    for (uint64_t b0 = uint64_t(blockIdx.x) * blockDim.x * kU + threadIdx.x; b0 < kc.n; b0 += step) {
+        int32_t key[kU];
+        bool    ok[kU];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) ok[u] = load_key(kc, b0 + uint64_t(u) * blockDim.x, key[u]);
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            if (ok[u]) {
+                atomicAdd(hist + uint32_t(bucket_of(fib_hash(key[u]), R)), 1u);
+                ++mine;
+            }
         }
     }
     __syncthreads();
@@ -211,11 +216,12 @@ __device__ __forceinline__ bool chunk_range(uint32_t cid, const uint32_t* chunk_
 // old value.  Lanes of a warp that all carry one slot (a Zipf-heavy key fills
 // whole chunks) need one atomic; otherwise each lane adds on its own.
 __device__ __forceinline__ uint32_t bucket_add(uint32_t* addr, uint32_t slot, unsigned act) {
-    uint32_t     first = 0;
-    const bool   uni   = __match_all_sync(act, slot, reinterpret_cast<int*>(&first)) != 0;
-    const unsigned lane = threadIdx.x & 31;
+    const unsigned lane   = threadIdx.x & 31;
+    const int      leader = __ffs(act) - 1;
+    // uniform when every active lane carries the leader's slot (a shuffle and
+    // a vote: cheaper than a match instruction)
+    const bool uni = __all_sync(act, slot == __shfl_sync(act, slot, leader));
     if (uni) {
-        const int leader = __ffs(act) - 1;
         uint32_t  base   = 0;
         if (int(lane) == leader) base = atomicAdd(addr + slot, uint32_t(__popc(act)));
         return __shfl_sync(act, base, leader) + __popc(act & ((1u << lane) - 1));
@@ -239,22 +245,31 @@ __global__ void __launch_bounds__(kThreads)
     for (uint32_t i = threadIdx.x; i < 2 * nl; i += blockDim.x) sh[i] = 0;
     __syncthreads();
     const uint32_t lmask = nl - 1;
-    for (uint32_t w0 = s + (threadIdx.x & ~31u); w0 < e; w0 += blockDim.x) {
-        const uint32_t j  = w0 + (threadIdx.x & 31);
-        const bool     ok = j < e;
-        const unsigned act = __ballot_sync(0xffffffffu, ok);
-        if (ok) {
-            const uint64_t h     = fib_hash(tkey[j]);
-            const uint32_t local = uint32_t(bucket_of(h, g.b)) & lmask;
-            bucket_add(cnt, local, act);
-            // a warp of one heavy key ORs its tags once, not 32 times on one word
-            uint32_t   first = 0;
-            const bool uni   = __match_all_sync(act, local, reinterpret_cast<int*>(&first)) != 0;
-            if (uni) {
-                const uint32_t all = __reduce_or_sync(act, bloom_mask(h));
-                if (int(threadIdx.x & 31) == __ffs(act) - 1) atomicOr(blm + local, all);
-            } else {
-                atomicOr(blm + local, bloom_mask(h));
+    constexpr int  kU    = 8;  // keys per thread loaded before any of them is counted
+    for (uint32_t b0 = s; b0 < e; b0 += kU * blockDim.x) {
+        int32_t key[kU];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            const uint32_t j = b0 + uint32_t(u) * blockDim.x + threadIdx.x;
+            key[u]           = j < e ? __ldg(tkey + j) : 0;
+        }
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            const uint32_t j   = b0 + uint32_t(u) * blockDim.x + threadIdx.x;
+            const bool     ok  = j < e;
+            const unsigned act = __ballot_sync(0xffffffffu, ok);
+            if (ok) {
+                const uint64_t h      = fib_hash(key[u]);
+                const uint32_t local  = uint32_t(bucket_of(h, g.b)) & lmask;
+                const int      leader = __ffs(act) - 1;
+                bucket_add(cnt, local, act);
+                // a warp of one heavy key ORs its tags once, not 32 times on one word
+                if (__all_sync(act, local == __shfl_sync(act, local, leader))) {
+                    const uint32_t all = __reduce_or_sync(act, bloom_mask(h));
+                    if (int(threadIdx.x & 31) == leader) atomicOr(blm + local, all);
+                } else {
+                    atomicOr(blm + local, bloom_mask(h));
+                }
             }
         }
     }
@@ -319,15 +334,19 @@ __global__ void __launch_bounds__(kThreads, 2)
     __syncthreads();
     const uint32_t lmask = nl - 1;
     int32_t        keys[kItems];
-    uint32_t       loc[kItems];
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) {
+        const uint32_t j = s + uint32_t(k) * kThreads + threadIdx.x;
+        keys[k]          = j < e ? __ldg(tkey + j) : 0;
+        // the rows are stored after the counts: bring their lines into L1 now
+        if (j < e) asm volatile("prefetch.global.L1 [%0];" ::"l"(trow + j));
+    }
 #pragma unroll
     for (int k = 0; k < kItems; ++k) {
         const uint32_t j  = s + uint32_t(k) * kThreads + threadIdx.x;
         const bool     ok = j < e;
-        keys[k]           = ok ? tkey[j] : 0;
-        loc[k]            = ok ? (uint32_t(bucket_of(fib_hash(keys[k]), g.b)) & lmask) : 0;
         const unsigned act = __ballot_sync(0xffffffffu, ok);
-        if (ok) bucket_add(sh, loc[k], act);
+        if (ok) bucket_add(sh, uint32_t(bucket_of(fib_hash(keys[k]), g.b)) & lmask, act);
     }
     __syncthreads();
     const uint64_t gb = uint64_t(part) << g.L;
@@ -341,7 +360,7 @@ __global__ void __launch_bounds__(kThreads, 2)
         const bool     ok  = j < e;
         const unsigned act = __ballot_sync(0xffffffffu, ok);
         if (ok) {
-            const uint32_t pos = bucket_add(sh, loc[k], act);
+            const uint32_t pos = bucket_add(sh, uint32_t(bucket_of(fib_hash(keys[k]), g.b)) & lmask, act);
             okey[pos]          = keys[k];
             orow[pos]          = trow[j];
         }
@@ -355,7 +374,9 @@ __global__ void __launch_bounds__(kThreads, 2)
 // each); the mixed bits come from neighbouring keys of the placed order.
 // Larger partitions (Zipf-heavy keys) take the chunked kernels, which skip the
 // partitions handled here.
-constexpr int kLT = 1024;  // threads of k_bucket_local
+constexpr int kLT = 1024;            // threads of k_bucket_local
+constexpr int kLU = kFuseMax / kLT;  // tuples per thread of a partition it takes, at most
+static_assert(kLU * kLT == int(kFuseMax), "a partition is one pass of the block");
 
 __global__ void __launch_bounds__(kLT, 1)
     k_bucket_local(Geo g, const uint32_t* __restrict__ part_off, const int32_t* __restrict__ tkey,
@@ -380,17 +401,34 @@ __global__ void __launch_bounds__(kLT, 1)
         const uint64_t gb = uint64_t(part) << g.L;
         for (uint32_t i = threadIdx.x; i < nl + nbw + nmw; i += blockDim.x) sh[i] = 0;
         __syncthreads();
+        // the partition's keys, all loaded before any is counted (kLU per thread)
+        int32_t key[kLU];
+#pragma unroll
+        for (int u = 0; u < kLU; ++u) {
+            const uint32_t j = s + uint32_t(u) * kLT + threadIdx.x;
+            key[u]           = j < e ? __ldg(tkey + j) : 0;
+        }
+        const int nu = int((e - s + kLT - 1) / kLT);  // passes of the block that hold tuples
         // counts and Bloom tags
-        for (uint32_t w0 = s + (threadIdx.x & ~31u); w0 < e; w0 += blockDim.x) {
-            const uint32_t j   = w0 + lane;
+#pragma unroll
+        for (int u = 0; u < kLU; ++u) {
+            if (u >= nu) break;
+            const uint32_t j   = s + uint32_t(u) * kLT + threadIdx.x;
             const bool     ok  = j < e;
             const unsigned act = __ballot_sync(0xffffffffu, ok);
             if (ok) {
-                const uint64_t h     = fib_hash(tkey[j]);
+                const uint64_t h     = fib_hash(key[u]);
                 const uint32_t local = uint32_t(bucket_of(h, g.b)) & lmask;
                 bucket_add(cnt, local, act);
                 atomicOr(blm + (local >> 1), bloom_mask(h) << (16 * (local & 1)));
             }
+        }
+        // the rows are placed after the scan: their loads overlap it
+        uint32_t row[kLU];
+#pragma unroll
+        for (int u = 0; u < kLU; ++u) {
+            const uint32_t j = s + uint32_t(u) * kLT + threadIdx.x;
+            row[u]           = j < e ? __ldg(trow + j) : 0u;
         }
         __syncthreads();
         // exclusive scan of the counts: warp w scans segments of 32 counts
@@ -419,16 +457,17 @@ __global__ void __launch_bounds__(kLT, 1)
         }
         __syncthreads();
         // place the tuples in bucket order
-        for (uint32_t w0 = s + (threadIdx.x & ~31u); w0 < e; w0 += blockDim.x) {
-            const uint32_t j   = w0 + lane;
+#pragma unroll
+        for (int u = 0; u < kLU; ++u) {
+            if (u >= nu) break;
+            const uint32_t j   = s + uint32_t(u) * kLT + threadIdx.x;
             const bool     ok  = j < e;
             const unsigned act = __ballot_sync(0xffffffffu, ok);
             if (ok) {
-                const int32_t  k     = tkey[j];
-                const uint32_t local = uint32_t(bucket_of(fib_hash(k), g.b)) & lmask;
+                const uint32_t local = uint32_t(bucket_of(fib_hash(key[u]), g.b)) & lmask;
                 const uint32_t q     = bucket_add(cnt, local, act) - s;
-                sk[q]                = k;
-                sr[q]                = trow[j];
+                sk[q]                = key[u];
+                sr[q]                = row[u];
             }
         }
         __syncthreads();

@@ -33,9 +33,77 @@ __global__ void k_page_rows(const uint8_t* __restrict__ pages, uint64_t num_page
     rows[p] = r;
 }
 
-// One warp per page (grid-stride over pages), 4 x 32 rows at a time: each
-// non-NULL row's rank among the page's non-NULL rows comes from ballots of the
-// bitmap bits, so no block-wide barrier is needed.  The bitmap bytes of the 4
+// INT32 pages: one block per page (grid-stride over pages).  The page, which
+// is almost all values and bitmap, is copied into
+// shared memory with one 16-byte load per thread per 4 KB (all in flight
+// together); a warp scan of the bitmap words' popcounts gives every 32-row
+// group its first non-NULL rank; then thread t decodes rows t, t + 256, ...
+// from shared memory (rank = group base + popcount of the lower bits) and
+// stores them coalesced.  No global load depends on another.
+constexpr uint32_t kMaxWords = (kPage * 8 + 31) / 32;  // bitmap words of a page, at most
+
+struct PageSmem {
+    uint4    img[kPage / 16];
+    uint32_t base[kMaxWords];  // non-NULL rows before each 32-row group
+};
+
+// Copies page `pg` into s.img and fills s.base for its nr rows; returns the
+// bitmap's byte offset within the page.  Ends with a block barrier.
+__device__ __forceinline__ uint32_t stage_page(const uint8_t* __restrict__ pg, uint32_t nr, PageSmem& s) {
+    const uint4* src = reinterpret_cast<const uint4*>(pg);
+    uint4        v[kPage / 16 / kDecThreads];
+#pragma unroll
+    for (int k = 0; k < kPage / 16 / kDecThreads; ++k) v[k] = __ldg(src + threadIdx.x + k * kDecThreads);
+#pragma unroll
+    for (int k = 0; k < kPage / 16 / kDecThreads; ++k) s.img[threadIdx.x + k * kDecThreads] = v[k];
+    __syncthreads();
+    const uint8_t* b    = reinterpret_cast<const uint8_t*>(s.img);
+    const uint32_t bm0  = kPage - (nr + 7) / 8;
+    const uint32_t nw   = (nr + 31) / 32;
+    if (threadIdx.x < 32) {
+        uint32_t run = 0;
+        for (uint32_t w0 = 0; w0 < nw; w0 += 32) {
+            const uint32_t w = w0 + threadIdx.x;
+            uint32_t       c = 0;
+            if (w < nw) {
+                // bits of rows 32w .. 32w + 31 (bytes past the page's rows are 0 or masked)
+                uint32_t word = 0;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const uint32_t byte = 4 * w + k;
+                    if (bm0 + byte < kPage) word |= uint32_t(b[bm0 + byte]) << (8 * k);
+                }
+                const uint32_t valid = nr - 32 * w >= 32 ? 0xffffffffu : ((1u << (nr - 32 * w)) - 1u);
+                c = __popc(word & valid);
+            }
+            const uint32_t inc = warp_inclusive_scan<uint32_t>(c);
+            if (w < nw) s.base[w] = run + inc - c;
+            run += __shfl_sync(0xffffffffu, inc, 31);
+        }
+    }
+    __syncthreads();
+    return bm0;
+}
+
+// Row i of the staged page: its validity and non-NULL rank.
+__device__ __forceinline__ bool row_rank(const PageSmem& s, uint32_t bm0, uint32_t i, uint32_t& rank) {
+    const uint8_t* b    = reinterpret_cast<const uint8_t*>(s.img);
+    const uint32_t w    = i >> 5, l = i & 31;
+    uint32_t       word = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const uint32_t byte = 4 * w + k;
+        if (bm0 + byte < kPage) word |= uint32_t(b[bm0 + byte]) << (8 * k);
+    }
+    rank = s.base[w] + __popc(word & ((1u << l) - 1u));
+    return (word >> l) & 1u;
+}
+
+// VARCHAR pages: one warp per page (grid-stride over pages), 4 x 32 rows at a
+// time -- only the offsets and the bitmap are read, never the string bytes,
+// which make up most of such a page.  Each non-NULL row's rank among the
+// page's non-NULL rows comes from ballots of the bitmap bits, so no
+// block-wide barrier is needed.  The bitmap bytes of the 4
 // steps are loaded together, then the 4 values (fetch), then stored, so each
 // lane has 4 independent loads in flight instead of one dependent chain.
 template <class Fetch, class Store>
@@ -78,19 +146,20 @@ __device__ __forceinline__ uint64_t total_warps() { return (uint64_t(gridDim.x) 
 __global__ void __launch_bounds__(kDecThreads)
     k_decode_int32_tagged(const uint8_t* __restrict__ pages, uint64_t num_pages,
                           const uint64_t* __restrict__ row_start, uint64_t* __restrict__ out) {
-    for (uint64_t p = global_warp(); p < num_pages; p += total_warps()) {
-        const uint8_t* pg   = pages + p * kPage;
-        const uint32_t nr   = *reinterpret_cast<const uint16_t*>(pg);
-        const int32_t* data = reinterpret_cast<const int32_t*>(pg + 4);
+    __shared__ PageSmem s;
+    for (uint64_t p = blockIdx.x; p < num_pages; p += gridDim.x) {
+        const uint8_t* pg  = pages + p * kPage;
+        const uint32_t nr  = *reinterpret_cast<const uint16_t*>(pg);
+        const uint32_t bm0 = stage_page(pg, nr, s);
+        const int32_t* data = reinterpret_cast<const int32_t*>(reinterpret_cast<const uint8_t*>(s.img) + 4);
         uint64_t*      o    = out + row_start[p];
-        warp_rows(
-            pg, nr,
-            [&](bool on, uint32_t rank) {
-                // a well-formed page has rank < num_non_null <= 2047; never read past it
-                return (on && rank < (kPage - 4) / 4) ? (uint64_t(uint32_t(__ldg(data + rank))) | value_t::TAG_INT32)
-                                                      : 0ull;
-            },
-            [&](uint32_t i, uint64_t v) { o[i] = v; });
+        for (uint32_t i = threadIdx.x; i < nr; i += kDecThreads) {
+            uint32_t   rank;
+            const bool on = row_rank(s, bm0, i, rank);
+            // a well-formed page has rank < num_non_null <= 2047; never read past it
+            o[i] = (on && rank < (kPage - 4) / 4) ? (uint64_t(uint32_t(data[rank])) | value_t::TAG_INT32) : 0ull;
+        }
+        __syncthreads();  // the next page overwrites the image
     }
 }
 
@@ -135,6 +204,11 @@ __global__ void __launch_bounds__(kDecThreads, 8)
     }
 }
 
+// one block per page
+unsigned block_page_grid(uint64_t num_pages) {
+    return unsigned(std::max<uint64_t>(1, std::min<uint64_t>(num_pages, uint64_t(num_sms()) * 8)));
+}
+
 // one warp per page: kDecThreads / 32 pages per block
 unsigned page_grid(uint64_t num_pages) {
     const uint64_t blocks = (num_pages + kDecThreads / 32 - 1) / (kDecThreads / 32);
@@ -152,7 +226,7 @@ void launch_page_rows(const uint8_t* pages, uint64_t num_pages, int32_t type, ui
 void launch_decode_int32_tagged(const uint8_t* pages, uint64_t num_pages, const uint64_t* row_start,
                                 uint64_t* out, cudaStream_t st) {
     if (num_pages == 0) return;
-    k_decode_int32_tagged<<<page_grid(num_pages), kDecThreads, 0, st>>>(pages, num_pages, row_start, out);
+    k_decode_int32_tagged<<<block_page_grid(num_pages), kDecThreads, 0, st>>>(pages, num_pages, row_start, out);
     HJ_LAUNCH_CHECK();
 }
 

@@ -350,7 +350,7 @@ struct hj_context {
     std::string         err;
     int64_t             dir_bits    = -1;
     int64_t             radix_bits  = -1;
-    int64_t             probe_group = 8;
+    int64_t             probe_group = 4;
     int64_t             light_max   = 32;
     int64_t             timing      = 0;
     int64_t             dir_cap_bits = 23;  // automatic directories stay <= 64 MB (L2 resident)

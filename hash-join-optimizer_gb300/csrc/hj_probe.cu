@@ -22,21 +22,27 @@
 //            the matching tuples as a 32-bit mask over the bucket and stages
 //            the hit with the uniform ones; larger buckets go to a list
 //            counted by a warp or block per hit (k_mixed_count*).
-// Staged hits are compacted with warp ballot/popc into shared memory.  Per
-// tile, ONE global 64-bit atomic reserves both the hits' list slots (high
-// word) and their output rows (low word), and a block scan of the staged
-// counts gives each hit its first output row, so list order and output order
-// agree and no device-wide prefix sum is needed (the reference's per-thread
-// work-stealing counter becomes this per-block reservation).
+// A hit stays in the registers of the thread that found it.  Within a warp,
+// hits are ordered round by round (the eight keys of a thread are eight
+// rounds), so a ballot ranks a round's hits into consecutive list slots
+// (coalesced stores) and a warp scan of their match counts gives their first
+// output rows.  The kernel keeps its shared memory small (the two key
+// stages): the rest of the SM's 256 KB stays L1, where the summaries of
+// frequently probed buckets are cached.  Per tile,
+// ONE global 64-bit atomic reserves both the block's list slots (high word)
+// and its output rows (low word), so list order and output order agree and no
+// device-wide prefix sum is needed (the reference's per-thread work-stealing
+// counter becomes this per-block reservation).
 //
 // Write pass.  k_write_uniform walks the OUTPUT positions in chunks of
-// 256 x G (G outputs per thread, option probe_group): a chunk's hits are
-// located by the chunk map (k_chunk_first), a uniform hit's bucket start is
-// read from its directory word, each thread finds its hit by binary search in
-// shared memory and reads build rows rows[start + k] consecutively, and every
-// output row-id stream is written with coalesced stores through a
-// shared-memory image.  Work is balanced by output
-// rows, so one Zipf-heavy key with millions of tuples spreads over all SMs.
+// 32 x G per warp (G outputs per thread, option probe_group): a chunk's hits
+// are located by the chunk map (k_chunk_first) and staged in the warp's own
+// shared memory, a uniform hit's bucket start is read from its directory
+// word, each thread finds its hit by binary search and reads build rows
+// rows[start + k] consecutively, and writes its G row ids of every output
+// stream as one 16-byte store (a warp covers 512 contiguous bytes).  Warps
+// synchronise only with themselves.  Work is balanced by output rows, so one
+// Zipf-heavy key with millions of tuples spreads over all SMs.
 // Mixed hits follow the uniform ones.  Every match writes one row id per
 // requested output stream, composed through the sides' row-id vectors (late
 // materialisation).
@@ -157,29 +163,27 @@ __device__ __forceinline__ bool tile_key(const KeyCol& pk, const uint8_t* stage,
 }
 
 template <int SRC>
-__global__ void __launch_bounds__(kPT)
+__global__ void __launch_bounds__(kPT, 4)
     k_probe_count(ProbeTab T, KeyCol pk, int light_max, Lists Ls, uint64_t ntiles) {
     extern __shared__ __align__(128) uint8_t dyn[];
-    constexpr uint32_t SB    = stage_bytes(SRC);
-    constexpr uint32_t kCap  = uint32_t(kPT) * kStep;                       // staged hits per tile
-    uint8_t*           stg   = dyn;                                          // 2 stages
-    uint32_t*          s_row = reinterpret_cast<uint32_t*>(dyn + 2 * SB);    // kCap each
-    uint32_t*          s_sp  = s_row + kCap;
-    uint32_t*          s_cnt = s_sp + kCap;
-    uint32_t*          s_msk = s_cnt + kCap;
+    constexpr uint32_t SB  = stage_bytes(SRC);
+    constexpr int      kW  = kPT / 32;
+    uint8_t*           stg = dyn;  // 2 stages
     __shared__ uint64_t bar[2];
-    __shared__ uint32_t s_n, s_fail, s_cov;
-    __shared__ unsigned long long s_base, s_red[33];
-    const unsigned lane = threadIdx.x & 31;
+    __shared__ uint32_t s_cov;
+    // per warp: staged hits and their matches (mod 2^32), turned into the
+    // warp's bases within the tile by thread 0; exact match counts
+    __shared__ uint32_t           s_wh[kW], s_wc[kW];
+    __shared__ unsigned long long s_wx[kW];
+    __shared__ uint32_t           s_hb, s_ob;
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned lt   = (1u << lane) - 1;
     uint32_t       cov0 = 0, cov1 = 0;   // thread 0: rows each stage's copy covers
     uint32_t       iss0 = 0, iss1 = 0;   // thread 0: copies issued into each stage
-    if (threadIdx.x == 0) {
-        s_n    = 0;
-        s_fail = 0;
-        if (SRC != kSrcGather) {
-            mbar_init(&bar[0]);
-            mbar_init(&bar[1]);
-        }
+    bool           gave_up = false;  // a staging wait ran out of polls (an error)
+    if (SRC != kSrcGather && threadIdx.x == 0) {
+        mbar_init(&bar[0]);
+        mbar_init(&bar[1]);
     }
     __syncthreads();
     if (SRC != kSrcGather && threadIdx.x == 0 && uint64_t(blockIdx.x) < ntiles) {
@@ -192,17 +196,20 @@ __global__ void __launch_bounds__(kPT)
         const uint32_t st = k & 1;
         if (SRC != kSrcGather) {
             // the other stage was last read before the previous iteration's
-            // closing barrier: refill it with the next tile now
+            // barriers: refill it with the next tile now
             const uint64_t next = tile + gridDim.x;
             if (threadIdx.x == 0 && next < ntiles) {
                 const uint32_t c = stage_tile<SRC>(pk, next, stg + (st ^ 1) * SB, &bar[st ^ 1]);
                 if (st) { cov0 = c; ++iss0; } else { cov1 = c; ++iss1; }
             }
-            if (!mbar_wait_bounded(&bar[st], (k >> 1) & 1, kWaitPolls)) s_fail = 1;
+            gave_up = !mbar_wait_bounded(&bar[st], (k >> 1) & 1, kWaitPolls);
             // thread 0 holds the covered counts; every thread needs this tile's
             if (threadIdx.x == 0) s_cov = st ? cov1 : cov0;
-            __syncthreads();
-            if (s_fail) break;
+        }
+        // one barrier that also tells every thread whether any gave up
+        if (__syncthreads_or(gave_up)) {
+            gave_up = true;
+            break;
         }
         const uint32_t cov   = SRC != kSrcGather ? s_cov : 0u;
         const uint64_t r0    = tile * kTileRows;
@@ -218,56 +225,46 @@ __global__ void __launch_bounds__(kPT)
             key[it]          = 0;
             w[it]            = 0;
             if (i < nrows) ok[it] = tile_key<SRC>(pk, stage, cov, i, r0 + i, key[it]);
+            // through L1: with skewed probe keys the hot buckets' summaries stay there
             if (ok[it]) w[it] = __ldg(T.sum + bucket_of(fib_hash(key[it]), T.b));
         }
-        // classify: 0 miss, 1 uniform, 2 mixed.  Directory words are read only
-        // for mixed buckets and for uniform buckets whose length saturated
-        // the summary's field
-        uint32_t s[kStep], e[kStep], L[kStep];
+        // classify: 0 miss, 1 hit staged here, 2 mixed bucket counted later.
+        // Directory words are read only for mixed buckets and for uniform
+        // buckets whose length saturated the summary's field.
+        uint32_t s[kStep], L[kStep], msk[kStep];
         int      cls[kStep];
 #pragma unroll
         for (int it = 0; it < kStep; ++it) {
             const uint64_t h = fib_hash(key[it]);
-            const uint32_t m = bloom_mask(h);
             L[it]            = sum_len(w[it]);
+            msk[it]          = 0;
             cls[it]          = 0;
-            if (ok[it] && L[it] != 0 && (sum_bloom(w[it]) & m) == m)
-                cls[it] = sum_mixed(w[it]) ? 2 : (sum_head(w[it]) == key[it] ? 1 : 0);
+            if (ok[it] && L[it] != 0) {
+                if (!sum_mixed(w[it])) {
+                    // a bucket of one key: its first key decides exactly (a matching
+                    // key's Bloom bits are always in the bucket's tag)
+                    cls[it] = sum_head(w[it]) == key[it] ? 1 : 0;
+                } else {
+                    const uint32_t m = bloom_mask(h);
+                    cls[it]          = (sum_bloom(w[it]) & m) == m ? 2 : 0;
+                }
+            }
             const uint64_t p = bucket_of(h, T.b);
             s[it]            = uint32_t(p);
-            e[it]            = 0;
+            uint32_t e       = 0;
             if (cls[it] == 2 || (cls[it] == 1 && L[it] == kSumLenMax)) {
                 const uint32_t b0 = uint32_t(__ldg(T.dir + p) >> 16);
                 L[it]             = uint32_t(__ldg(T.dir + p + 1) >> 16) - b0;
                 if (cls[it] == 2) s[it] = b0;
-                e[it] = b0 + L[it];
+                e = b0 + L[it];
             }
-        }
-#pragma unroll
-        for (int it = 0; it < kStep; ++it) {
-            const uint32_t i = uint32_t(it) * kPT + threadIdx.x;
-            const uint64_t j = r0 + i;
             // a small mixed bucket: compared here, its matches as a mask
-            uint32_t msk = 0, c = L[it];
             if (cls[it] == 2 && L[it] <= small) {
-                for (uint32_t q = 0; q < L[it]; ++q) msk |= uint32_t(__ldg(T.keys + s[it] + q) == key[it]) << q;
-                c       = __popc(msk);
-                cls[it] = c ? 1 : 0;
-            }
-            // staged in shared memory in lane order: (row, bucket or first
-            // tuple, count, mask)
-            {
-                const unsigned bal = __ballot_sync(0xffffffffu, cls[it] == 1);
-                uint32_t       q0  = 0;
-                if (lane == 0 && bal) q0 = atomicAdd(&s_n, uint32_t(__popc(bal)));
-                q0 = __shfl_sync(0xffffffffu, q0, 0);
-                if (cls[it] == 1) {
-                    const uint32_t q = q0 + __popc(bal & ((1u << lane) - 1));
-                    s_row[q]         = uint32_t(j);
-                    s_sp[q]          = s[it];
-                    s_cnt[q]         = c;
-                    s_msk[q]         = msk;
-                }
+                uint32_t mm = 0;
+                for (uint32_t q = 0; q < L[it]; ++q) mm |= uint32_t(__ldg(T.keys + s[it] + q) == key[it]) << q;
+                msk[it] = mm;
+                L[it]   = __popc(mm);
+                cls[it] = mm ? 1 : 0;
             }
             // larger mixed buckets: counted later; rare, so warp-aggregated
             // global atomics
@@ -277,61 +274,97 @@ __global__ void __launch_bounds__(kPT)
                 if (lane == 0) q0 = atomicAdd(Ls.ctr + 1, (unsigned long long)__popc(bal));
                 q0 = __shfl_sync(0xffffffffu, q0, 0);
                 if (cls[it] == 2) {
-                    const uint64_t q = q0 + __popc(bal & ((1u << lane) - 1));
-                    Ls.m_row[q]      = uint32_t(j);
+                    const uint64_t q = q0 + __popc(bal & lt);
+                    Ls.m_row[q]      = uint32_t(r0 + uint32_t(it) * kPT + threadIdx.x);
                     Ls.m_s[q]        = s[it];
-                    Ls.m_e[q]        = e[it];
+                    Ls.m_e[q]        = e;
                     Ls.m_key[q]      = key[it];
                     Ls.m_cnt[q]      = kUncounted;
                 }
             }
         }
-        __syncthreads();
-        // output rows of the staged hits: exclusive prefix of their counts in
-        // staging order.  Warp w scans entries 256 w .. 256 w + 255 in rows of
-        // 32 (lane i reads entry 32 q + i: no bank conflicts), leaving each
-        // entry's prefix within its warp in s_cnt; then the warps' totals.
-        const uint32_t nst  = s_n;
-        const uint32_t warp = threadIdx.x >> 5;
-        uint64_t       wsum = 0;
+        // the warp's hits in (it, lane) order, so the hits of one round are
+        // consecutive list slots (coalesced stores): per round a ballot ranks
+        // them and a warp scan of their counts gives their first output rows
+        // within the warp -- a ballot suffices when no hit has more than one
+        // match (32-bit prefix sums; the exact total is summed beside them)
+        uint32_t           nh = 0, nc = 0;
+        unsigned long long lx = 0;
+        uint32_t           slot[kStep], oo[kStep];
+        static_assert(kStep % 2 == 0, "rounds are scanned in pairs");
 #pragma unroll
-        for (int q = 0; q < kStep; ++q) {
-            const uint32_t x   = (warp * kStep + q) * 32 + lane;
-            const uint32_t c   = x < nst ? s_cnt[x] : 0u;
-            const uint64_t inc = warp_inclusive_scan<uint64_t>(c);
-            if (x < nst) s_cnt[x] = uint32_t(wsum + inc - c);
-            wsum += __shfl_sync(0xffffffffu, inc, 31);
+        for (int it = 0; it < kStep; it += 2) {
+            const bool     h0 = cls[it] == 1, h1 = cls[it + 1] == 1;
+            const uint32_t c0 = h0 ? L[it] : 0u, c1 = h1 ? L[it + 1] : 0u;
+            const unsigned b0 = __ballot_sync(0xffffffffu, h0), b1 = __ballot_sync(0xffffffffu, h1);
+            const uint32_t r0 = __popc(b0 & lt), r1 = __popc(b1 & lt);
+            slot[it]          = nh + r0;
+            slot[it + 1]      = nh + __popc(b0) + r1;
+            nh += __popc(b0) + __popc(b1);
+            if (!__any_sync(0xffffffffu, (c0 | c1) > 1)) {  // one match per hit: the ranks
+                oo[it]     = nc + r0;
+                oo[it + 1] = nc + __popc(b0) + r1;
+                nc += __popc(b0) + __popc(b1);
+            } else if (__all_sync(0xffffffffu, (c0 | c1) < 2048)) {
+                // both rounds in one scan of 16-bit halves (a half sums to < 2^16)
+                const uint32_t v   = c0 | (c1 << 16);
+                const uint32_t inc = warp_inclusive_scan<uint32_t>(v);
+                const uint32_t tot = __shfl_sync(0xffffffffu, inc, 31);
+                const uint32_t ex  = inc - v;
+                oo[it]             = nc + (ex & 0xffffu);
+                oo[it + 1]         = nc + (tot & 0xffffu) + (ex >> 16);
+                nc += (tot & 0xffffu) + (tot >> 16);
+            } else {
+                const uint32_t i0 = warp_inclusive_scan<uint32_t>(c0);
+                oo[it]            = nc + i0 - c0;
+                nc += __shfl_sync(0xffffffffu, i0, 31);
+                const uint32_t i1 = warp_inclusive_scan<uint32_t>(c1);
+                oo[it + 1]        = nc + i1 - c1;
+                nc += __shfl_sync(0xffffffffu, i1, 31);
+            }
+            lx += uint64_t(c0) + c1;
         }
-        if (lane == 0) s_red[warp] = wsum;
+        const unsigned long long nx = warp_sum<unsigned long long>(lx);
+        if (lane == 0) {
+            s_wh[warp] = nh;
+            s_wc[warp] = nc;
+            s_wx[warp] = nx;
+        }
         __syncthreads();
         if (threadIdx.x == 0) {
-            unsigned long long tile_sum = 0;
-            for (int w = 0; w < kPT / 32; ++w) {
-                const unsigned long long x = s_red[w];
-                s_red[w]                   = tile_sum;  // warp bases
-                tile_sum += x;
+            uint32_t           hs = 0, cs = 0;
+            unsigned long long xs = 0;
+#pragma unroll
+            for (int q = 0; q < kW; ++q) {
+                const uint32_t h = s_wh[q], c = s_wc[q];
+                s_wh[q] = hs;
+                s_wc[q] = cs;
+                hs += h;
+                cs += c;
+                xs += s_wx[q];
             }
-            // one reservation: list slots in the high word, output rows in the
-            // low word (mod 2^32; the exact total is summed beside it)
-            s_base = nst ? atomicAdd(Ls.ctr + 0, (uint64_t(nst) << 32) + (tile_sum & 0xffffffffull)) : 0ull;
-            if (tile_sum) atomicAdd(Ls.ctr + 2, tile_sum);
+            const unsigned long long base = hs ? atomicAdd(Ls.ctr + 0, (uint64_t(hs) << 32) + cs) : 0ull;
+            if (xs) atomicAdd(Ls.ctr + 2, xs);
+            s_hb = uint32_t(base >> 32);
+            s_ob = uint32_t(base);
         }
         __syncthreads();
-        const uint32_t hb = uint32_t(s_base >> 32), ob = uint32_t(s_base);
-        for (uint32_t x = threadIdx.x; x < nst; x += blockDim.x) {
-            Ls.u_row[hb + x]  = s_row[x];
-            Ls.u_sp[hb + x]   = s_sp[x];
-            Ls.u_off[hb + x]  = ob + uint32_t(s_red[x >> 8]) + s_cnt[x];
-            Ls.u_mask[hb + x] = s_msk[x];
+        const uint32_t hb = s_hb + s_wh[warp], ob = s_ob + s_wc[warp];
+#pragma unroll
+        for (int it = 0; it < kStep; ++it) {
+            if (cls[it] == 1) {
+                const uint32_t q = hb + slot[it];
+                Ls.u_row[q]      = uint32_t(r0 + uint32_t(it) * kPT + threadIdx.x);
+                Ls.u_sp[q]       = s[it];
+                Ls.u_off[q]      = ob + oo[it];
+                Ls.u_mask[q]     = msk[it];
+            }
         }
-        __syncthreads();
-        if (threadIdx.x == 0) s_n = 0;
-        __syncthreads();
     }
     if (SRC != kSrcGather) {
         // a block that gave up waits (bounded) for the copies it issued, so no
         // copy lands in shared memory after the block has exited
-        if (s_fail && threadIdx.x == 0) {
+        if (gave_up && threadIdx.x == 0) {
             atomicAdd(Ls.ctr + 4, 1ull);
             if (iss0) mbar_wait_bounded(&bar[0], (iss0 - 1) & 1, kWaitPolls);
             if (iss1) mbar_wait_bounded(&bar[1], (iss1 - 1) & 1, kWaitPolls);
@@ -401,11 +434,13 @@ __global__ void k_chunk_first(const uint32_t* __restrict__ off, uint64_t n_u, ui
     if (c < nchunks) chunk_first[c] = uint32_t(hit_of(off, n_u, c * chunk));
 }
 
-// Shared memory of k_write_uniform<G>: one output stream's image, then the
-// chunk's hits (at most chunk + 1: every hit holds at least one output, plus
-// the hit that starts at the next chunk's first position): relative starts
-// (chunk + 2), probe rows, tuple starts, unclamped relative starts and masks.
-constexpr size_t write_uniform_smem(int G) { return (6 * (size_t(256) * G) + 6) * sizeof(uint32_t); }
+// Outputs of one warp's chunk in k_write_uniform<G>, and the per-warp
+// shared memory: the chunk's hits (at most chunk + 1: every hit holds at least
+// one output, plus the hit that starts at the next chunk's first position):
+// relative starts (chunk + 2), probe rows, tuple starts, unclamped relative
+// starts and masks.
+constexpr uint32_t warp_chunk(int G) { return 32u * uint32_t(G); }
+constexpr size_t   write_uniform_smem(int G) { return 8 * 5 * (size_t(warp_chunk(G)) + 2) * sizeof(uint32_t); }
 
 // Index of the k-th set bit of m (k < popcount(m)).
 __device__ __forceinline__ uint32_t nth_bit(uint32_t m, uint32_t k) {
@@ -413,32 +448,49 @@ __device__ __forceinline__ uint32_t nth_bit(uint32_t m, uint32_t k) {
     return uint32_t(__ffs(m) - 1);
 }
 
+// G consecutive values to dst (16-byte aligned runs of 4 as vector stores).
 template <int G>
-__global__ void __launch_bounds__(256)
+__device__ __forceinline__ void store_run(uint32_t* dst, const uint32_t (&v)[G], bool vec, uint64_t pol) {
+    if (G >= 4 && vec) {
+#pragma unroll
+        for (int i = 0; i < G; i += 4)
+            st_hint(reinterpret_cast<uint4*>(dst + i), make_uint4(v[i], v[i + 1], v[i + 2], v[i + 3]), pol);
+    } else if (G == 2 && vec) {
+        *reinterpret_cast<uint2*>(dst) = make_uint2(v[0], v[G > 1 ? 1 : 0]);
+    } else {
+#pragma unroll
+        for (int i = 0; i < G; ++i) dst[i] = v[i];
+    }
+}
+
+template <int G>
+__global__ void __launch_bounds__(256, G <= 4 ? 6 : (G <= 8 ? 4 : 2))
     k_write_uniform(ProbeTab T, Lists Ls, uint64_t n_u, const uint32_t* __restrict__ chunk_first, uint64_t total,
                     Outs outs) {
     const uint32_t* __restrict__ off = Ls.u_off;
-    constexpr uint32_t CH = 256u * G;
+    constexpr uint32_t CH = warp_chunk(G);
+    constexpr uint32_t NW = CH + 2;
     extern __shared__ __align__(16) uint32_t wsh[];
-    uint32_t* s_val  = wsh;               // CH: one output stream
-    uint32_t* s_rel  = s_val + CH;        // CH + 2: hit starts relative to the chunk, clamped to [0, len]
-    uint32_t* s_pr   = s_rel + CH + 2;    // CH + 1: probe row of each hit
-    uint32_t* s_s    = s_pr + CH + 1;     // CH + 1: first tuple of each hit's bucket
-    uint32_t* s_orel = s_s + CH + 1;      // CH + 1: hit start - chunk start, mod 2^32
-    uint32_t* s_msk  = s_orel + CH + 1;   // CH + 1: match mask (0: every tuple)
-    __shared__ uint64_t s_h[2];
+    const unsigned lane  = threadIdx.x & 31;
+    uint32_t*      s_rel  = wsh + (threadIdx.x >> 5) * 5 * NW;  // hit starts relative to the chunk, clamped to [0, len]
+    uint32_t*      s_pr   = s_rel + NW;                         // probe row of each hit
+    uint32_t*      s_s    = s_pr + NW;                          // first tuple of each hit's bucket
+    uint32_t*      s_orel = s_s + NW;                           // hit start - chunk start, mod 2^32
+    uint32_t*      s_msk  = s_orel + NW;                        // match mask (0: every tuple)
+    // vector stores need every stream 16-byte aligned (engine buffers are)
+    bool vec = true;
+    for (int oi = 0; oi < outs.n; ++oi) vec &= (reinterpret_cast<uintptr_t>(outs.o[oi].dst) & 15) == 0;
     const uint64_t nchunks = (total + CH - 1) / CH;
-    for (uint64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+    const uint64_t nw      = (uint64_t(gridDim.x) * blockDim.x) >> 5;
+    const uint64_t stream  = l2_evict_first();  // row ids are written once, read later in order
+    for (uint64_t c = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; c < nchunks; c += nw) {
         const uint64_t o0  = c * CH;
         const uint32_t len = uint32_t(umin64(CH, total - o0));
-        if (threadIdx.x == 0) {
-            s_h[0] = chunk_first ? chunk_first[c] : hit_of(off, n_u, o0);
-            s_h[1] = c + 1 < nchunks ? (chunk_first ? chunk_first[c + 1] : hit_of(off, n_u, o0 + CH)) : n_u - 1;
-        }
-        __syncthreads();
-        const uint64_t h0 = s_h[0];
-        const uint32_t nh = uint32_t(s_h[1] - h0) + 1;  // hits h0 .. h0 + nh - 1 cover the chunk
-        for (uint32_t q = threadIdx.x; q <= nh; q += blockDim.x) {
+        const uint64_t h0  = chunk_first ? __ldg(chunk_first + c) : hit_of(off, n_u, o0);
+        const uint64_t h1  = c + 1 < nchunks ? (chunk_first ? __ldg(chunk_first + c + 1) : hit_of(off, n_u, o0 + CH))
+                                             : n_u - 1;
+        const uint32_t nh  = uint32_t(h1 - h0) + 1;  // hits h0 .. h0 + nh - 1 cover the chunk
+        for (uint32_t q = lane; q <= nh; q += 32) {
             const uint64_t hq  = h0 + q;
             const uint64_t o   = hq < n_u ? uint64_t(__ldg(off + hq)) : total;
             const uint64_t rel = o > o0 ? o - o0 : 0;
@@ -453,10 +505,10 @@ __global__ void __launch_bounds__(256)
                 s_msk[q]  = m;
             }
         }
-        __syncthreads();
-        const uint32_t q0 = threadIdx.x * G;
-        uint32_t       prow[G], brow[G];
+        __syncwarp();
+        const uint32_t q0 = lane * G;
         if (q0 < len) {
+            uint32_t prow[G], brow[G];
             uint32_t lo = 0, hi = nh;  // largest k with s_rel[k] <= q0
             while (hi - lo > 1) {
                 const uint32_t mid = (lo + hi) >> 1;
@@ -467,6 +519,7 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
             for (int i = 0; i < G; ++i) {
                 const uint32_t q = q0 + i;
+                prow[i] = brow[i] = 0;
                 if (q < len) {
                     while (s_rel[k + 1] <= q) ++k;
                     const uint32_t idx = q - s_orel[k];  // match number within the hit
@@ -475,27 +528,26 @@ __global__ void __launch_bounds__(256)
                     brow[i]            = __ldg(T.rows + s_s[k] + (m ? nth_bit(m, idx) : idx));
                 }
             }
-        }
-        for (int oi = 0; oi < outs.n; ++oi) {
-            const RidOut o = outs.o[oi];
-            if (q0 < len) {
+            const bool full = q0 + G <= len;
+            for (int oi = 0; oi < outs.n; ++oi) {
+                const RidOut o = outs.o[oi];
+                uint32_t     v[G];
 #pragma unroll
                 for (int i = 0; i < G; ++i) {
-                    if (q0 + i < len) {
-                        const uint32_t x = o.side == 0 ? prow[i] : brow[i];
-                        s_val[q0 + i]    = o.src ? __ldg(o.src + x) : x;
-                    }
+                    const uint32_t x = o.side == 0 ? prow[i] : brow[i];
+                    v[i]             = (o.src && q0 + i < len) ? __ldg(o.src + x) : x;
+                }
+                uint32_t* dst = o.dst + o0 + q0;
+                if (full) {
+                    store_run<G>(dst, v, vec, stream);
+                } else {
+#pragma unroll
+                    for (int i = 0; i < G; ++i)
+                        if (q0 + i < len) dst[i] = v[i];
                 }
             }
-            __syncthreads();
-            uint32_t*      dst = o.dst + o0;
-            // 16-byte stores where the caller's buffer allows (engine buffers always do)
-            const uint32_t n4  = (reinterpret_cast<uintptr_t>(dst) & 15) ? 0u : len / 4;
-            for (uint32_t v = threadIdx.x; v < n4; v += blockDim.x)
-                reinterpret_cast<uint4*>(dst)[v] = reinterpret_cast<const uint4*>(s_val)[v];
-            for (uint32_t v = 4 * n4 + threadIdx.x; v < len; v += blockDim.x) dst[v] = s_val[v];
-            __syncthreads();
         }
+        __syncwarp();  // the next chunk's hits overwrite this warp's shared memory
     }
 }
 
@@ -561,8 +613,11 @@ int key_source(const KeyCol& pk) {
 template <int SRC>
 void launch_count_src(const ProbeTab& T, const KeyCol& pk, int light_max, const Lists& L, cudaStream_t st) {
     const uint64_t ntiles = (pk.n + kTileRows - 1) / kTileRows;
-    const size_t   smem   = 2 * size_t(stage_bytes(SRC)) + 4 * size_t(kPT) * kStep * sizeof(uint32_t);
+    const size_t   smem   = std::max<size_t>(16, 2 * size_t(stage_bytes(SRC)));
     HJ_CUDA(cudaFuncSetAttribute(k_probe_count<SRC>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    // shared memory for the resident blocks only; the rest of the unified
+    // L1 / shared memory caches bucket summaries
+    HJ_CUDA(cudaFuncSetAttribute(k_probe_count<SRC>, cudaFuncAttributePreferredSharedMemoryCarveout, 30));
     // resident blocks walk the tiles (each prefetching its next tile)
     int per_sm = 0;
     HJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_probe_count<SRC>, kPT, smem));
@@ -604,8 +659,8 @@ void launch_uniform_g(const ProbeTab& T, const Lists& L, uint64_t n_u, const uin
     HJ_CUDA(cudaFuncSetAttribute(k_write_uniform<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     int per_sm = 0;
     HJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_write_uniform<G>, 256, smem));
-    const uint64_t nchunks = (total + 256u * G - 1) / (256u * G);
-    const uint64_t grid    = std::max<uint64_t>(1, std::min<uint64_t>(nchunks, uint64_t(num_sms()) * std::max(1, per_sm)));
+    const uint64_t nchunks = (total + warp_chunk(G) - 1) / warp_chunk(G);
+    const uint64_t grid    = std::max<uint64_t>(1, std::min<uint64_t>((nchunks + 7) / 8, uint64_t(num_sms()) * std::max(1, per_sm)));
     k_write_uniform<G><<<unsigned(grid), 256, smem, st>>>(T, L, n_u, chunk_first, total, outs);
     HJ_LAUNCH_CHECK();
 }
@@ -693,7 +748,7 @@ void probe_write(const Table& t, const KeyCol& pk, ProbePlan* pp, const RidOut* 
     Lists&         L = pp->ls;
     if (pp->n_u) {
         const int      G       = writer_items(pp->group);
-        const uint64_t chunk   = 256u * uint64_t(G);
+        const uint64_t chunk   = warp_chunk(G);
         const uint64_t nchunks = (pp->tot_u + chunk - 1) / chunk;
         uint32_t*      cfirst  = dalloc_n<uint32_t>(nchunks + 1, st);
         k_chunk_first<<<div_up(nchunks, 256), 256, 0, st>>>(L.u_off, pp->n_u, nchunks, uint32_t(chunk), cfirst);

@@ -48,6 +48,24 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t b
         : "memory");
 }
 
+// L2 cache policy (createpolicy) for stores of lines written once and read
+// back later in order (output row ids): they leave L2 first.
+__device__ __forceinline__ uint64_t l2_evict_first() {
+    uint64_t p;
+    asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+
+// 16-byte and 4-byte stores with an L2 cache policy.
+__device__ __forceinline__ void st_hint(uint4* p, uint4 v, uint64_t policy) {
+    asm volatile("st.global.L2::cache_hint.v4.u32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(p), "r"(v.x), "r"(v.y), "r"(v.z),
+                 "r"(v.w), "l"(policy)
+                 : "memory");
+}
+__device__ __forceinline__ void st_hint(uint32_t* p, uint32_t v, uint64_t policy) {
+    asm volatile("st.global.L2::cache_hint.u32 [%0], %1, %2;" ::"l"(p), "r"(v), "l"(policy) : "memory");
+}
+
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
     uint32_t done;
     asm volatile(

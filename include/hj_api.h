@@ -151,7 +151,7 @@ void* hj_context_stream(hj_context* ctx);
  * 64 MB, cache resident; results do not depend on it), "radix_bits" (partition fan-out of the
  * build, 0..12), "probe_group" (output rows per thread of the match writer,
  * so a probe key's matches spread over count / probe_group threads: 1, 2, 4,
- * 8 (default), 16 or 32), "light_max" (a bucket of several keys with at most
+ * 8, 16 or 32; default 4), "light_max" (a bucket of several keys with at most
  * this many tuples is compared by the probing thread itself; larger ones by a
  * warp or block per hit), "timing" (1: record per-phase device times of
  * each hj_execute, read with hj_result_phase_ms), "host_access" (1, default:
