@@ -304,25 +304,44 @@ __device__ __forceinline__ uint64_t page_rec(uint32_t row, uint32_t nn, uint32_t
 __global__ void __launch_bounds__(kPackT) k_pack_count(PackCols P, uint64_t ntiles) {
     __shared__ uint32_t sm[33];
     __shared__ uint64_t s_scan[33];
+    __shared__ uint64_t s_loc[kStrTile];  // the tile's locators in row order
     for (uint64_t g = blockIdx.x; g < ntiles; g += gridDim.x) {
         const PackCol& v  = P.c[pack_col_of(P, g)];
         const uint64_t t  = g - v.tile_base;
         const uint64_t t0 = t * kStrTile, t1 = (v.n < t0 + kStrTile ? v.n : t0 + kStrTile);
+        const uint32_t nt = uint32_t(t1 - t0);
+        // gather with coalesced row ids (rows k * kPackT + thread): all row ids
+        // first, then all locators, then the stores in output order
+        {
+            uint32_t src[kPackRow];
+            uint64_t lg[kPackRow];
+#pragma unroll
+            for (int k = 0; k < kPackRow; ++k) {
+                const uint32_t li = uint32_t(k) * kPackT + threadIdx.x;
+                src[k]            = li < nt ? (v.rid ? __ldg(v.rid + t0 + li) : uint32_t(t0 + li)) : 0u;
+            }
+#pragma unroll
+            for (int k = 0; k < kPackRow; ++k) {
+                const uint32_t li = uint32_t(k) * kPackT + threadIdx.x;
+                lg[k]             = li < nt ? __ldg(v.locs + (v.rid ? uint64_t(src[k]) : t0 + li)) : 0ull;
+            }
+#pragma unroll
+            for (int k = 0; k < kPackRow; ++k) {
+                const uint32_t li = uint32_t(k) * kPackT + threadIdx.x;
+                if (li < nt) v.ol[t0 + li] = lg[k];
+                s_loc[li] = lg[k];
+            }
+        }
+        __syncthreads();
+        // packing: thread t takes the tile's rows t * kPackRow .. + kPackRow - 1
         const uint64_t r0 = t0 + uint64_t(threadIdx.x) * kPackRow;
         const uint32_t rows = r0 >= t1 ? 0u : (t1 - r0 < kPackRow ? uint32_t(t1 - r0) : uint32_t(kPackRow));
         uint64_t*      rec  = v.recs + t * kRec;
         uint64_t       loc[kPackRow];
 #pragma unroll
-        for (int k = 0; k < kPackRow; ++k) {
-            loc[k] = 0;
-            if (uint32_t(k) < rows) {
-                const uint64_t i = r0 + k;
-                loc[k]           = __ldg(v.locs + (v.rid ? uint64_t(__ldg(v.rid + i)) : i));
-                v.ol[i]          = loc[k];
-            }
-        }
+        for (int k = 0; k < kPackRow; ++k) loc[k] = s_loc[threadIdx.x * kPackRow + k];  // 0 past the tile's rows
         TileCosts c = row_costs(loc, rows);
-        tile_max_any(c.maxc, c.greedy, sm);  // (its barriers also publish ol to the block)
+        tile_max_any(c.maxc, c.greedy, sm);
         if (c.greedy) {
             if (threadIdx.x < 32) {
                 const uint32_t np = pack_tile(v.ol, v.base, v.npages, t0, t1, nullptr);
@@ -343,7 +362,7 @@ __global__ void __launch_bounds__(kPackT) k_pack_count(PackCols P, uint64_t ntil
         uint32_t       NN = uint32_t(pre >> 40), LEN = uint32_t(pre & ((1ull << 40) - 1));
         // S: the row's start in eighths of a byte (offsets, string bytes, one bit per row)
         uint32_t S       = 8u * (2u * NN + LEN) + li0;
-        uint32_t pg_prev = li0 > 0 && rows > 0 ? (S - loc_cost(v.ol[r0 - 1])) / T : 0u;
+        uint32_t pg_prev = li0 > 0 && rows > 0 ? (S - loc_cost(s_loc[li0 - 1])) / T : 0u;
 #pragma unroll
         for (int k = 0; k < kPackRow; ++k) {
             if (uint32_t(k) >= rows) break;
