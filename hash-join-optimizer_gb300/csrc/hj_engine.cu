@@ -255,6 +255,9 @@ struct DevColumn {
     uint64_t non_null  = 0;
     bool     dense1984 = false;  // INT32, no NULLs, every page but the last 1984 rows
     int64_t  strref_bad_page = -1;  // first page index > 2^18-1 that carries strings
+    // first row of each page (num_pages + 1 words), from the headers at upload,
+    // for columns that are decoded (not dense INT32)
+    Buf row_start;
     // decoded form (per execute call, or once per resident table: predecoded)
     bool decoded    = false;
     bool predecoded = false;
@@ -467,6 +470,27 @@ void download_pages(hj_context* c, const uint8_t* src, uint64_t n, void* const* 
     drain();
 }
 
+// The first row of every page of a column that the decode kernels read (INT32
+// that is not dense, VARCHAR), summed on the host from the page headers it
+// has already read at upload, and copied to the device once.
+void page_row_starts(hj_context* c, DevColumn& d, const uint16_t* nr) {
+    if (d.num_pages == 0 || (d.type == HJ_INT32 && d.dense1984) || (d.type != HJ_INT32 && d.type != HJ_VARCHAR))
+        return;
+    std::vector<uint64_t> rs(d.num_pages + 1);
+    uint64_t              run = 0;
+    for (uint64_t p = 0; p < d.num_pages; ++p) {
+        rs[p]      = run;
+        uint32_t r = nr[p];
+        if (d.type == HJ_VARCHAR) r = nr[p] == 0xffff ? 1u : (nr[p] == 0xfffe ? 0u : nr[p]);
+        run += r;
+    }
+    rs[d.num_pages] = run;
+    d.row_start     = make_buf(rs.size() * sizeof(uint64_t), c->st);
+    HJ_CUDA(cudaMemcpyAsync(d.row_start->p, rs.data(), rs.size() * sizeof(uint64_t), cudaMemcpyHostToDevice, c->st));
+    // the source is pageable and local: the copy must have read it before return
+    HJ_CUDA(cudaStreamSynchronize(c->st));
+}
+
 bool direct_host_access(const hj_context* c) { return c->ats_capable && c->host_access; }
 
 // Uploads the listed columns of a host table (others stay empty).  Pages in
@@ -513,6 +537,7 @@ std::shared_ptr<DevTable> upload_table(hj_context* c, const hj_table_desc& t,
         nn.assign(d.num_pages, 0);
         upload_pages(c, t.columns[i].pages, d.num_pages, d.pages->as<uint8_t>(), nr.data(), nn.data());
         page_stats(d, nr.data(), nn.data());
+        page_row_starts(c, d, nr.data());
     }
     std::vector<std::vector<uint16_t>> hnr(t.num_columns), hnn(t.num_columns);
     bool                               any = false;
@@ -527,7 +552,10 @@ std::shared_ptr<DevTable> upload_table(hj_context* c, const hj_table_desc& t,
     }
     if (any) HJ_CUDA(cudaStreamSynchronize(c->st));
     for (uint32_t i = 0; i < t.num_columns; ++i) {
-        if (dhdr[i]) page_stats(dt->cols[i], hnr[i].data(), hnn[i].data());
+        if (dhdr[i]) {
+            page_stats(dt->cols[i], hnr[i].data(), hnn[i].data());
+            page_row_starts(c, dt->cols[i], hnr[i].data());
+        }
         const DevColumn& d = dt->cols[i];
         if (d.pages && std::getenv("HJ_TRACE_UPLOAD"))
             std::fprintf(stderr, "[hj upload] column %u type %d pages %llu rows %llu non_null %llu dense1984 %d\n", i,
@@ -571,10 +599,14 @@ void decode_kernels(cudaStream_t st, DevColumn& d) {
     if (!d.pages) throw Error(HJ_ERR_INVALID, "column pages were not uploaded");
     if (d.type == HJ_INT32 && d.dense1984) return;  // read in place (direct mode)
     const uint64_t np = d.num_pages;
-    uint32_t*      pr = dalloc_n<uint32_t>(np, st);
-    uint64_t*      rs = dalloc_n<uint64_t>(np + 1, st);
-    launch_page_rows(d.pages->as<uint8_t>(), np, d.type, pr, st);
-    scan_exclusive_u32_to_u64(pr, rs, np, st);
+    uint32_t*      pr = nullptr;
+    uint64_t*      rs = d.row_start ? d.row_start->as<uint64_t>() : nullptr;
+    if (!rs) {  // a column without host page statistics: row starts on the device
+        pr = dalloc_n<uint32_t>(np, st);
+        rs = dalloc_n<uint64_t>(np + 1, st);
+        launch_page_rows(d.pages->as<uint8_t>(), np, d.type, pr, st);
+        scan_exclusive_u32_to_u64(pr, rs, np, st);
+    }
     if (d.type == HJ_INT32 && d.non_null == d.rows) {
         d.plain = make_buf(d.rows * 4, st);
         launch_decode_int32_plain(d.pages->as<uint8_t>(), np, rs, d.plain->as<int32_t>(), st);
@@ -585,8 +617,10 @@ void decode_kernels(cudaStream_t st, DevColumn& d) {
         d.locs = make_buf(d.rows * 8, st);
         launch_decode_varchar_loc(d.pages->as<uint8_t>(), np, rs, d.locs->as<uint64_t>(), st);
     }
-    dfree(pr, st);
-    dfree(rs, st);
+    if (pr) {
+        dfree(pr, st);
+        dfree(rs, st);
+    }
 }
 
 // ------------------------------------------------------------ intermediates --
