@@ -327,27 +327,40 @@ def run_e2e(args, d: Dist, hj, eng, w, npr: int, out_pages: list, stream) -> dic
         if depth > 1:
             srv = hj.Server(eng, hbm_budget_bytes=int(args.budget_gb * 2**30), slots=depth)
             try:
+                # per plan, to see where overlap is lost: its upload (device time),
+                # its time in a slot (upload + execute) and the client's fetch
+                seen = {"upload_ms": [], "service_ms": [], "fetch_ms": []}
+
+                def finish(ticket):
+                    r, st = srv.wait(ticket)
+                    seen["upload_ms"].append(eng.stats(r)[3].get("upload", 0.0))
+                    seen["service_ms"].append(st["service_ms"])
+                    t0 = time.perf_counter()
+                    fetch(r)
+                    seen["fetch_ms"].append(1e3 * (time.perf_counter() - t0))
+                    eng.free_result(r)
+
                 def pipelined(k):
                     q = collections.deque()
                     for _ in range(k):
                         q.append(srv.submit(w.plan))
                         if len(q) >= depth:
-                            r, _st = srv.wait(q.popleft())
-                            fetch(r)
-                            eng.free_result(r)
+                            finish(q.popleft())
                     while q:
-                        r, _st = srv.wait(q.popleft())
-                        fetch(r)
-                        eng.free_result(r)
+                        finish(q.popleft())
                 kp = max(k2, 3 * depth)
                 # warm the slots: each slot's first plans set up its stream's pools
                 for _ in range(2):
                     pipelined(kp)
+                for v in seen.values():
+                    v.clear()
                 pipe_ms, pipe_blocks = timed(pipelined, kp)
             finally:
                 srv.close()
             modes["pipelined"] = {"ms_per_step": pipe_ms, "plans_in_flight": depth,
-                                  "blocks_ms_per_step": [round(x, 3) for x in pipe_blocks]}
+                                  "blocks_ms_per_step": [round(x, 3) for x in pipe_blocks],
+                                  "median_per_plan_ms": {k: round(sorted(v)[len(v) // 2], 3)
+                                                         for k, v in seen.items() if v}}
             if pipe_ms < serial_ms:
                 out.update({"value": npr * d.world / (pipe_ms / 1e3), "ms_per_step": pipe_ms,
                             "mode": f"pipelined through hj_server, {depth} plans in flight"})
