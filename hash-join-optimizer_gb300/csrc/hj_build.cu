@@ -39,6 +39,9 @@ constexpr int kThreads     = 512;
 constexpr int kItems       = 16;
 constexpr int kTile        = kThreads * kItems;  // rows per partition-scatter tile
 constexpr int kChunk       = kTile;              // tuples per bucket chunk
+// Partitions of at most kFuseMax tuples are built by one block each
+// (k_bucket_local); the chunked kernels take the larger ones.
+constexpr uint32_t kFuseMax = 12288;
 
 struct Geo {
     uint32_t b;  // directory bits
@@ -82,16 +85,20 @@ __global__ void __launch_bounds__(kThreads)
     if ((threadIdx.x & 31) == 0 && mine) atomicAdd(n_valid, (unsigned long long)mine);
 }
 
-// 2. Exclusive scans of partition sizes and chunk counts (one block).
+// 2. Exclusive scans of partition sizes and chunk counts (one block).  Only
+//    the partitions k_bucket_local does not take are cut into chunks; each
+//    chunk's partition is written to chunk_part, so a chunk kernel's block
+//    finds its partition with one load.
 __global__ void __launch_bounds__(1024)
     k_part_offsets(const uint32_t* __restrict__ part_cnt, uint32_t P, uint32_t* __restrict__ part_off,
-                   uint32_t* __restrict__ part_cursor, uint32_t* __restrict__ chunk_off) {
+                   uint32_t* __restrict__ part_cursor, uint32_t* __restrict__ chunk_off,
+                   uint32_t* __restrict__ chunk_part) {
     __shared__ uint32_t sm[33];
     uint32_t            run_t = 0, run_c = 0;
     for (uint32_t base = 0; base < P; base += blockDim.x) {
         const uint32_t i  = base + threadIdx.x;
         const uint32_t c  = i < P ? part_cnt[i] : 0;
-        const uint32_t ch = (c + kChunk - 1) / kChunk;
+        const uint32_t ch = c > kFuseMax ? (c + kChunk - 1) / kChunk : 0u;
         uint32_t       tot_t, tot_c;
         const uint32_t et = block_exclusive_scan<uint32_t>(c, sm, &tot_t);
         const uint32_t ec = block_exclusive_scan<uint32_t>(ch, sm, &tot_c);
@@ -107,6 +114,9 @@ __global__ void __launch_bounds__(1024)
         part_off[P]  = run_t;
         chunk_off[P] = run_c;
     }
+    __syncthreads();
+    for (uint32_t p = threadIdx.x; p < P; p += blockDim.x)
+        for (uint32_t c = chunk_off[p]; c < chunk_off[p + 1]; ++c) chunk_part[c] = p;
 }
 
 // 3. Scatter (key, row) to partitions.  Each block owns a tile of kTile rows:
@@ -132,15 +142,18 @@ __global__ void __launch_bounds__(kST, 1024 / kST)
     for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) off[i] = 0;
     __syncthreads();
     int32_t  keys[kItems];
-    uint32_t parts[kItems], rank[kItems];
+    uint32_t rank[kItems];
     uint32_t okmask = 0;
+    // all of the thread's keys are loaded before any is counted
 #pragma unroll
     for (int k = 0; k < kItems; ++k) {
-        const uint64_t i   = tile0 + uint64_t(k) * kST + threadIdx.x;
-        const bool     ok  = load_key(kc, i, keys[k]);
-        parts[k]           = ok ? uint32_t(bucket_of(fib_hash(keys[k]), R)) : 0;
-        rank[k]            = ok ? atomicAdd(off + parts[k], 1u) : 0;
-        okmask |= uint32_t(ok) << k;
+        const uint64_t i = tile0 + uint64_t(k) * kST + threadIdx.x;
+        okmask |= uint32_t(load_key(kc, i, keys[k])) << k;
+    }
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) {
+        const bool ok = (okmask >> k) & 1u;
+        rank[k]       = ok ? atomicAdd(off + uint32_t(bucket_of(fib_hash(keys[k]), R)), 1u) : 0;
     }
     __syncthreads();
     // exclusive scan of the counts (thread t: partitions [t * per, (t + 1) * per))
@@ -169,10 +182,11 @@ __global__ void __launch_bounds__(kST, 1024 / kST)
 #pragma unroll
     for (int k = 0; k < kItems; ++k) {
         if ((okmask >> k) & 1u) {
-            const uint32_t q = off[parts[k]] + rank[k];
-            sk[q]            = keys[k];
-            sr[q]            = uint32_t(tile0 + uint64_t(k) * kST + threadIdx.x);
-            sp[q]            = uint16_t(parts[k]);
+            const uint32_t part = uint32_t(bucket_of(fib_hash(keys[k]), R));  // recomputed: fewer registers
+            const uint32_t q    = off[part] + rank[k];
+            sk[q]               = keys[k];
+            sr[q]               = uint32_t(tile0 + uint64_t(k) * kST + threadIdx.x);
+            sp[q]               = uint16_t(part);
         }
     }
     __syncthreads();
@@ -184,27 +198,17 @@ __global__ void __launch_bounds__(kST, 1024 / kST)
     }
 }
 
-// Partitions of at most kFuseMax tuples are built by one block each
-// (k_bucket_local); the chunked kernels take the larger ones.
-constexpr uint32_t kFuseMax = 12288;
 
 __device__ __forceinline__ bool fused_part(const uint32_t* part_off, uint32_t part) {
     return part_off[part + 1] - part_off[part] <= kFuseMax;
 }
 
 // Locates chunk `cid`: its partition and tuple range.  Returns false past the end.
-__device__ __forceinline__ bool chunk_range(uint32_t cid, const uint32_t* chunk_off,
+__device__ __forceinline__ bool chunk_range(uint32_t cid, const uint32_t* chunk_off, const uint32_t* chunk_part,
                                             const uint32_t* part_off, uint32_t P, uint32_t& part,
                                             uint32_t& s, uint32_t& e, bool& single) {
     if (cid >= chunk_off[P]) return false;
-    uint32_t lo = 0, hi = P;  // largest p with chunk_off[p] <= cid
-    while (hi - lo > 1) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (chunk_off[mid] <= cid) lo = mid;
-        else                       hi = mid;
-    }
-    // skip empty partitions that share the same chunk_off
-    part             = lo;
+    part             = chunk_part[cid];
     const uint32_t k = cid - chunk_off[part];
     s                = part_off[part] + k * kChunk;
     e                = min(part_off[part + 1], s + kChunk);
@@ -231,7 +235,8 @@ __device__ __forceinline__ uint32_t bucket_add(uint32_t* addr, uint32_t slot, un
 
 // 4. Per-chunk bucket counts and Bloom tags.
 __global__ void __launch_bounds__(kThreads)
-    k_bucket_count(Geo g, const uint32_t* __restrict__ chunk_off, const uint32_t* __restrict__ part_off,
+    k_bucket_count(Geo g, const uint32_t* __restrict__ chunk_off, const uint32_t* __restrict__ chunk_part,
+                   const uint32_t* __restrict__ part_off,
                    const int32_t* __restrict__ tkey, uint32_t* __restrict__ gcnt,
                    uint32_t* __restrict__ gbloom) {
     extern __shared__ uint32_t sh[];
@@ -240,7 +245,7 @@ __global__ void __launch_bounds__(kThreads)
     uint32_t*      blm = sh + nl;
     uint32_t       part, s, e;
     bool           single;
-    if (!chunk_range(blockIdx.x, chunk_off, part_off, 1u << g.R, part, s, e, single)) return;
+    if (!chunk_range(blockIdx.x, chunk_off, chunk_part, part_off, 1u << g.R, part, s, e, single)) return;
     if (fused_part(part_off, part)) return;  // k_bucket_local
     for (uint32_t i = threadIdx.x; i < 2 * nl; i += blockDim.x) sh[i] = 0;
     __syncthreads();
@@ -320,7 +325,8 @@ __global__ void __launch_bounds__(1024)
 
 // 6. Final scatter into bucket order.
 __global__ void __launch_bounds__(kThreads, 2)
-    k_bucket_scatter(Geo g, const uint32_t* __restrict__ chunk_off, const uint32_t* __restrict__ part_off,
+    k_bucket_scatter(Geo g, const uint32_t* __restrict__ chunk_off, const uint32_t* __restrict__ chunk_part,
+                     const uint32_t* __restrict__ part_off,
                      const int32_t* __restrict__ tkey, const uint32_t* __restrict__ trow,
                      uint32_t* __restrict__ cursor, int32_t* __restrict__ okey,
                      uint32_t* __restrict__ orow) {
@@ -328,7 +334,7 @@ __global__ void __launch_bounds__(kThreads, 2)
     const uint32_t nl = 1u << g.L;
     uint32_t       part, s, e;
     bool           single;
-    if (!chunk_range(blockIdx.x, chunk_off, part_off, 1u << g.R, part, s, e, single)) return;
+    if (!chunk_range(blockIdx.x, chunk_off, chunk_part, part_off, 1u << g.R, part, s, e, single)) return;
     if (fused_part(part_off, part)) return;  // k_bucket_local
     for (uint32_t i = threadIdx.x; i < nl; i += blockDim.x) sh[i] = 0;
     __syncthreads();
@@ -526,11 +532,12 @@ __global__ void __launch_bounds__(256)
 // 7. mixed[p] bit set when bucket p holds two different keys (chunks of the
 //    partitions k_bucket_local does not take).
 __global__ void __launch_bounds__(kThreads)
-    k_bucket_mixed(Geo g, const uint32_t* __restrict__ chunk_off, const uint32_t* __restrict__ part_off,
+    k_bucket_mixed(Geo g, const uint32_t* __restrict__ chunk_off, const uint32_t* __restrict__ chunk_part,
+                   const uint32_t* __restrict__ part_off,
                    const uint64_t* __restrict__ dir, const int32_t* __restrict__ key, uint32_t* __restrict__ mixed) {
     uint32_t part, s, e;
     bool     single;
-    if (!chunk_range(blockIdx.x, chunk_off, part_off, 1u << g.R, part, s, e, single)) return;
+    if (!chunk_range(blockIdx.x, chunk_off, chunk_part, part_off, 1u << g.R, part, s, e, single)) return;
     if (fused_part(part_off, part)) return;  // set by k_bucket_local
     // four tuples per thread at a time: keys, then directory words, then first keys
     for (uint32_t j0 = s + threadIdx.x; j0 < e; j0 += 4 * blockDim.x) {
@@ -630,7 +637,10 @@ void build_table(const KeyCol& kc, int dir_bits, int radix_bits, Table& t, uint6
     uint32_t* part_off    = dalloc_n<uint32_t>(P + 1, st);
     uint32_t* part_cursor = dalloc_n<uint32_t>(P, st);
     uint32_t* chunk_off   = dalloc_n<uint32_t>(P + 1, st);
-    k_part_offsets<<<1, 1024, 0, st>>>(part_cnt, P, part_off, part_cursor, chunk_off);
+    // chunks of the partitions above kFuseMax tuples, at most
+    const unsigned chunks_upper = unsigned((nv + kChunk - 1) / kChunk + nv / kFuseMax + 1);
+    uint32_t*      chunk_part   = dalloc_n<uint32_t>(chunks_upper, st);
+    k_part_offsets<<<1, 1024, 0, st>>>(part_cnt, P, part_off, part_cursor, chunk_off, chunk_part);
     HJ_LAUNCH_CHECK();
 
     int32_t*  tkey = dalloc_n<int32_t>(nv, st);
@@ -666,12 +676,11 @@ void build_table(const KeyCol& kc, int dir_bits, int radix_bits, Table& t, uint6
     HJ_CUDA(cudaMemsetAsync(gbloom, 0, nb * sizeof(uint32_t), st));
     HJ_CUDA(cudaMemsetAsync(t.mixed, 0, ((nb + 31) / 32) * sizeof(uint32_t), st));
 
-    const unsigned chunks_upper = unsigned((nv + kChunk - 1) / kChunk + P);
     {
         const size_t smem = 2 * (size_t(1) << g.L) * sizeof(uint32_t);
         HJ_CUDA(cudaFuncSetAttribute(k_bucket_count, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      int(smem)));
-        k_bucket_count<<<chunks_upper, kThreads, smem, st>>>(g, chunk_off, part_off, tkey, gcnt, gbloom);
+        k_bucket_count<<<chunks_upper, kThreads, smem, st>>>(g, chunk_off, chunk_part, part_off, tkey, gcnt, gbloom);
         HJ_LAUNCH_CHECK();
     }
     k_bucket_dir<<<P, 1024, 0, st>>>(g, part_off, gcnt, gbloom, t.dir);
@@ -689,17 +698,17 @@ void build_table(const KeyCol& kc, int dir_bits, int radix_bits, Table& t, uint6
         const size_t smem = (size_t(1) << g.L) * sizeof(uint32_t);
         HJ_CUDA(cudaFuncSetAttribute(k_bucket_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      int(smem)));
-        k_bucket_scatter<<<chunks_upper, kThreads, smem, st>>>(g, chunk_off, part_off, tkey, trow, gcnt,
+        k_bucket_scatter<<<chunks_upper, kThreads, smem, st>>>(g, chunk_off, chunk_part, part_off, tkey, trow, gcnt,
                                                               t.keys, t.rows);
         HJ_LAUNCH_CHECK();
     }
-    k_bucket_mixed<<<chunks_upper, kThreads, 0, st>>>(g, chunk_off, part_off, t.dir, t.keys, t.mixed);
+    k_bucket_mixed<<<chunks_upper, kThreads, 0, st>>>(g, chunk_off, chunk_part, part_off, t.dir, t.keys, t.mixed);
     HJ_LAUNCH_CHECK();
     k_bucket_summary<<<P, 256, 0, st>>>(g, part_off, t.dir, t.keys, t.mixed, t.summary);
     HJ_LAUNCH_CHECK();
 
     for (void* p : {(void*)d_nvalid, (void*)part_cnt, (void*)part_off, (void*)part_cursor,
-                    (void*)chunk_off, (void*)tkey, (void*)trow, (void*)gcnt, (void*)gbloom})
+                    (void*)chunk_off, (void*)chunk_part, (void*)tkey, (void*)trow, (void*)gcnt, (void*)gbloom})
         dfree(p, st);
 }
 
