@@ -68,6 +68,8 @@ def parse():
     ap.add_argument("--opt", action="append", default=[], metavar="NAME=VALUE",
                     help="engine option for the timed runs (hj_set_option), repeatable")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-systems", action="store_true",
+                    help="c2: leave out the batched and served summaries (c4 / c5 at reduced size)")
     ap.add_argument("--e2e-depth", type=int, default=3,
                     help="plans in flight in the pipelined end-to-end mode (1 = serial only)")
     ap.add_argument("--e2e-pageable", action="store_true",
@@ -619,6 +621,35 @@ def run_reference(args, d: Dist):
             "e2e": {"value": v, "unit": "probe tuples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def systems_summary(args, d: Dist) -> dict:
+    """The two systems forms at a reduced size, attached to the default c2 line
+    (one GPU) so that a plain `python bench.py` records them too: the batched
+    executor on the first 1,024 of the 4,096 c4 instances, and the serving loop
+    at 1,000 and 5,000 offered queries/s (200 requests each), both against the
+    plain one-query-at-a-time path on the same inputs.  `--workload c4|c5` runs
+    the full configurations."""
+    import copy
+    a = copy.copy(args)
+    a.instances, a.steps, a.warmup, a.scale = 1024, 3, 3, 1.0
+    b = run_batch(a, d)
+    a = copy.copy(args)
+    a.rates, a.requests, a.warmup, a.scale = "1000,5000", 200, 3, 1.0
+    v = run_serve(a, d)
+    top = v["rates"][-1]
+    return {
+        "batched": {"metric": b["metric"], "value": b["value"], "unit": b["unit"],
+                    "plain_value": b["plain"]["value"], "speedup_vs_plain": b["speedup_vs_plain"],
+                    "results_equal_plain": b["results_equal_plain"], "workload": b["config"]["workload"],
+                    "size": "1,024 of the 4,096 c4 instances", "steps": b["steps"]},
+        "served": {"metric": v["metric"], "value": v["value"], "unit": v["unit"],
+                   "offered_qps": top["offered_qps"], "plain_value": v["plain_qps_at_top_rate"],
+                   "speedup_vs_plain": v["speedup_vs_plain"], "p50_ms": top["served"]["p50_ms"],
+                   "p95_ms": top["served"]["p95_ms"], "p99_ms": top["served"]["p99_ms"],
+                   "plain_p99_ms": top["plain"]["p99_ms"], "results_equal": v["results_equal_plain"],
+                   "workload": v["config"]["workload"], "size": "200 requests per rate, rates 1,000 and 5,000 q/s"},
+    }
+
+
 def main():
     args = parse()
     d = Dist()
@@ -630,6 +661,9 @@ def main():
         line = run_serve(args, d)
     else:
         line = run_ours(args, d)
+        if (line is not None and args.workload == "c2" and args.scale == 1.0 and d.world == 1
+                and not args.no_systems):
+            line["systems"] = systems_summary(args, d)
     if d.rank == 0 and line is not None:
         print(json.dumps(line), flush=True)
     d.close()
