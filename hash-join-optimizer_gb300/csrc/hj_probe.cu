@@ -490,6 +490,49 @@ __global__ void __launch_bounds__(256, G <= 4 ? 6 : (G <= 8 ? 4 : 2))
         const uint64_t h1  = c + 1 < nchunks ? (chunk_first ? __ldg(chunk_first + c + 1) : hit_of(off, n_u, o0 + CH))
                                              : n_u - 1;
         const uint32_t nh  = uint32_t(h1 - h0) + 1;  // hits h0 .. h0 + nh - 1 cover the chunk
+        if (nh == 1) {
+            // the whole chunk inside one hit (the usual case for a Zipf-heavy
+            // key): lane 0 reads the hit, every lane takes consecutive matches
+            uint32_t orel = 0, m = 0, t0 = 0, prow = 0;
+            if (lane == 0) {
+                orel           = uint32_t(uint64_t(__ldg(off + h0)) - o0);  // mod 2^32: the hit may start earlier
+                m              = __ldg(Ls.u_mask + h0);
+                const uint32_t sp = __ldg(Ls.u_sp + h0);
+                prow           = __ldg(Ls.u_row + h0);
+                t0             = m ? sp : uint32_t(__ldg(T.dir + sp) >> 16);
+            }
+            orel = __shfl_sync(0xffffffffu, orel, 0);
+            m    = __shfl_sync(0xffffffffu, m, 0);
+            t0   = __shfl_sync(0xffffffffu, t0, 0);
+            prow = __shfl_sync(0xffffffffu, prow, 0);
+            const uint32_t q0 = lane * G;
+            if (q0 < len) {
+                uint32_t brow[G];
+#pragma unroll
+                for (int i = 0; i < G; ++i) {
+                    const uint32_t idx = q0 + i - orel;  // match number within the hit
+                    brow[i]            = q0 + i < len ? __ldg(T.rows + t0 + (m ? nth_bit(m, idx) : idx)) : 0u;
+                }
+                const bool full = q0 + G <= len;
+                for (int oi = 0; oi < outs.n; ++oi) {
+                    const RidOut o = outs.o[oi];
+                    uint32_t     v[G];
+                    const uint32_t pv = o.side == 0 ? (o.src ? __ldg(o.src + prow) : prow) : 0u;
+#pragma unroll
+                    for (int i = 0; i < G; ++i)
+                        v[i] = o.side == 0 ? pv : ((o.src && q0 + i < len) ? __ldg(o.src + brow[i]) : brow[i]);
+                    uint32_t* dst = o.dst + o0 + q0;
+                    if (full) {
+                        store_run<G>(dst, v, vec, stream);
+                    } else {
+#pragma unroll
+                        for (int i = 0; i < G; ++i)
+                            if (q0 + i < len) dst[i] = v[i];
+                    }
+                }
+            }
+            continue;
+        }
         for (uint32_t q = lane; q <= nh; q += 32) {
             const uint64_t hq  = h0 + q;
             const uint64_t o   = hq < n_u ? uint64_t(__ldg(off + hq)) : total;
@@ -634,10 +677,19 @@ void launch_count(const ProbeTab& T, const KeyCol& pk, int light_max, const List
     case kSrcTagged: launch_count_src<kSrcTagged>(T, pk, light_max, L, st); break;
     default: launch_count_src<kSrcGather>(T, pk, light_max, L, st); break;
     }
+}
+
+// After the counters were read back into host[0..4]: when the count pass
+// listed large mixed buckets (host[1] > 0), counts their matches and reads
+// their total back into host[3] (one more host wait; most tables have none).
+void count_mixed(const ProbeTab& T, const Lists& L, uint64_t* host, cudaStream_t st) {
+    if (host[1] == 0) return;
     k_mixed_count_warp<<<num_sms() * 4, 256, 0, st>>>(T, L);
     HJ_LAUNCH_CHECK();
     k_mixed_count<<<num_sms() * 2, 512, 0, st>>>(T, L);
     HJ_LAUNCH_CHECK();
+    readback(host + 3, L.ctr + 3, sizeof(uint64_t), true, st);  // page-locked scratch
+    HJ_CUDA(cudaStreamSynchronize(st));
 }
 
 // Outputs per thread of the uniform writer from option probe_group.
@@ -729,6 +781,7 @@ uint64_t probe_count(const Table& t, const KeyCol& pk, const ProbeParams& prm, P
     readback(pp->host, L.ctr, 5 * sizeof(uint64_t), true, st);  // page-locked scratch
     HJ_CUDA(cudaStreamSynchronize(st));
     check_staging(pp->host);
+    count_mixed(tab_of(t), L, pp->host, st);
     pp->n_u   = pp->host[0] >> 32;
     pp->n_m   = pp->host[1];
     pp->tot_u = pp->host[2];
@@ -816,6 +869,7 @@ int probe_into_scratch(const Table& t, const KeyCol& pk, const ProbeParams& prm,
     readback(h, L.ctr, 5 * sizeof(uint64_t), true, st);  // page-locked scratch
     HJ_CUDA(cudaStreamSynchronize(st));
     check_staging(h);
+    count_mixed(T, L, h, st);
     const uint64_t n_u = h[0] >> 32, n_m = h[1], tot_u = h[2], total = h[2] + h[3];
     *num_matches = total;
     if (total > capacity) return HJ_ERR_CAPACITY;
