@@ -38,7 +38,8 @@ constexpr int kMaxRadix    = 14;
 constexpr int kThreads     = 512;
 constexpr int kItems       = 16;
 constexpr int kTile        = kThreads * kItems;  // rows per partition-scatter tile
-constexpr int kChunk       = kTile;              // tuples per bucket chunk
+constexpr int kChunkTiles  = 1;
+constexpr int kChunk       = kChunkTiles * kTile;  // tuples per bucket chunk
 // Partitions of at most kFuseMax tuples are built by one block each
 // (k_bucket_local); the chunked kernels take the larger ones.
 constexpr uint32_t kFuseMax = 12288;
@@ -159,12 +160,21 @@ __global__ void __launch_bounds__(kST, 1024 / kST)
     // exclusive scan of the counts (thread t: partitions [t * per, (t + 1) * per))
     const uint32_t per = (P + kST - 1) / kST;
     uint32_t       run = 0;
-    for (uint32_t q = 0; q < per; ++q) {
-        const uint32_t p = threadIdx.x * per + q;
-        if (p < P) {
-            const uint32_t c = off[p];
-            gbase[p]         = c ? atomicAdd(part_cursor + p, c) : 0u;
+    // the thread's reservations four at a time, all four in flight before any
+    // result is stored
+    for (uint32_t q0 = 0; q0 < per; q0 += 4) {
+        uint32_t base[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const uint32_t q = q0 + u, p = threadIdx.x * per + q;
+            const uint32_t c = q < per && p < P ? off[p] : 0u;
+            base[u]          = c ? atomicAdd(part_cursor + p, c) : 0u;
             run += c;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const uint32_t q = q0 + u, p = threadIdx.x * per + q;
+            if (q < per && p < P) gbase[p] = base[u];
         }
     }
     uint32_t       tot;
@@ -231,6 +241,23 @@ __device__ __forceinline__ uint32_t bucket_add(uint32_t* addr, uint32_t slot, un
         return __shfl_sync(act, base, leader) + __popc(act & ((1u << lane) - 1));
     }
     return atomicAdd(addr + slot, 1u);
+}
+
+// Zeroes the bucket counters and Bloom tags of the partitions cut into more
+// than one chunk (k_bucket_count accumulates those with global atomics; a
+// single-chunk partition's are stored whole, and k_bucket_local's partitions
+// use neither).  One block per partition.
+__global__ void __launch_bounds__(256)
+    k_bucket_zero(Geo g, const uint32_t* __restrict__ chunk_off, const uint32_t* __restrict__ part_off,
+                  uint32_t* __restrict__ gcnt, uint32_t* __restrict__ gbloom) {
+    const uint32_t part = blockIdx.x;
+    if (fused_part(part_off, part) || chunk_off[part + 1] - chunk_off[part] <= 1) return;
+    const uint32_t nl = 1u << g.L;
+    const uint64_t gb = uint64_t(part) << g.L;
+    for (uint32_t i = threadIdx.x; i < nl; i += blockDim.x) {
+        gcnt[gb + i]   = 0;
+        gbloom[gb + i] = 0;
+    }
 }
 
 // 4. Per-chunk bucket counts and Bloom tags.
@@ -339,36 +366,64 @@ __global__ void __launch_bounds__(kThreads, 2)
     for (uint32_t i = threadIdx.x; i < nl; i += blockDim.x) sh[i] = 0;
     __syncthreads();
     const uint32_t lmask = nl - 1;
-    int32_t        keys[kItems];
+    // a chunk is kSub tiles of kTile tuples: all are counted, then placed
+    // (a one-tile chunk keeps its keys in registers between the two)
+    constexpr int kSub = kChunk / kTile;
+    int32_t       keys[kItems];
+    for (uint32_t b0 = s; b0 < e; b0 += kTile) {
 #pragma unroll
-    for (int k = 0; k < kItems; ++k) {
-        const uint32_t j = s + uint32_t(k) * kThreads + threadIdx.x;
-        keys[k]          = j < e ? __ldg(tkey + j) : 0;
-        // the rows are stored after the counts: bring their lines into L1 now
-        if (j < e) asm volatile("prefetch.global.L1 [%0];" ::"l"(trow + j));
-    }
+        for (int k = 0; k < kItems; ++k) {
+            const uint32_t j = b0 + uint32_t(k) * kThreads + threadIdx.x;
+            keys[k]          = j < e ? __ldg(tkey + j) : 0;
+            // the rows are stored after the counts: bring their lines into L1 now
+            if (kSub == 1 && j < e) asm volatile("prefetch.global.L1 [%0];" ::"l"(trow + j));
+        }
 #pragma unroll
-    for (int k = 0; k < kItems; ++k) {
-        const uint32_t j  = s + uint32_t(k) * kThreads + threadIdx.x;
-        const bool     ok = j < e;
-        const unsigned act = __ballot_sync(0xffffffffu, ok);
-        if (ok) bucket_add(sh, uint32_t(bucket_of(fib_hash(keys[k]), g.b)) & lmask, act);
+        for (int k = 0; k < kItems; ++k) {
+            const uint32_t j  = b0 + uint32_t(k) * kThreads + threadIdx.x;
+            const bool     ok = j < e;
+            const unsigned act = __ballot_sync(0xffffffffu, ok);
+            if (ok) bucket_add(sh, uint32_t(bucket_of(fib_hash(keys[k]), g.b)) & lmask, act);
+        }
     }
     __syncthreads();
     const uint64_t gb = uint64_t(part) << g.L;
-    for (uint32_t i = threadIdx.x; i < nl; i += blockDim.x) {
-        if (sh[i]) sh[i] = single ? cursor[gb + i] : atomicAdd(cursor + gb + i, sh[i]);
+    {
+        // the thread's buckets (at most 2^kLocalBits / kThreads): every cursor
+        // load or atomic issued before any result is stored
+        constexpr int kPer = (1 << kLocalBits) / kThreads;
+        uint32_t      c[kPer];
+#pragma unroll
+        for (int q = 0; q < kPer; ++q) {
+            const uint32_t i = threadIdx.x + uint32_t(q) * kThreads;
+            const uint32_t n = i < nl ? sh[i] : 0u;
+            c[q]             = n == 0 ? 0u : (single ? cursor[gb + i] : atomicAdd(cursor + gb + i, n));
+        }
+#pragma unroll
+        for (int q = 0; q < kPer; ++q) {
+            const uint32_t i = threadIdx.x + uint32_t(q) * kThreads;
+            if (i < nl && sh[i]) sh[i] = c[q];
+        }
     }
     __syncthreads();
+    for (uint32_t b0 = s; b0 < e; b0 += kTile) {
+        uint32_t rows[kItems];
 #pragma unroll
-    for (int k = 0; k < kItems; ++k) {
-        const uint32_t j   = s + uint32_t(k) * kThreads + threadIdx.x;
-        const bool     ok  = j < e;
-        const unsigned act = __ballot_sync(0xffffffffu, ok);
-        if (ok) {
-            const uint32_t pos = bucket_add(sh, uint32_t(bucket_of(fib_hash(keys[k]), g.b)) & lmask, act);
-            okey[pos]          = keys[k];
-            orow[pos]          = trow[j];
+        for (int k = 0; k < kItems; ++k) {
+            const uint32_t j = b0 + uint32_t(k) * kThreads + threadIdx.x;
+            if (kSub > 1) keys[k] = j < e ? __ldg(tkey + j) : 0;
+            rows[k] = j < e ? __ldg(trow + j) : 0u;
+        }
+#pragma unroll
+        for (int k = 0; k < kItems; ++k) {
+            const uint32_t j   = b0 + uint32_t(k) * kThreads + threadIdx.x;
+            const bool     ok  = j < e;
+            const unsigned act = __ballot_sync(0xffffffffu, ok);
+            if (ok) {
+                const uint32_t pos = bucket_add(sh, uint32_t(bucket_of(fib_hash(keys[k]), g.b)) & lmask, act);
+                okey[pos]          = keys[k];
+                orow[pos]          = rows[k];
+            }
         }
     }
 }
@@ -672,9 +727,9 @@ void build_table(const KeyCol& kc, int dir_bits, int radix_bits, Table& t, uint6
     t.summary             = dalloc_n<uint64_t>(nb, st);
     uint32_t* gcnt        = dalloc_n<uint32_t>(nb, st);
     uint32_t* gbloom      = dalloc_n<uint32_t>(nb, st);
-    HJ_CUDA(cudaMemsetAsync(gcnt, 0, nb * sizeof(uint32_t), st));
-    HJ_CUDA(cudaMemsetAsync(gbloom, 0, nb * sizeof(uint32_t), st));
     HJ_CUDA(cudaMemsetAsync(t.mixed, 0, ((nb + 31) / 32) * sizeof(uint32_t), st));
+    k_bucket_zero<<<P, 256, 0, st>>>(g, chunk_off, part_off, gcnt, gbloom);
+    HJ_LAUNCH_CHECK();
 
     {
         const size_t smem = 2 * (size_t(1) << g.L) * sizeof(uint32_t);

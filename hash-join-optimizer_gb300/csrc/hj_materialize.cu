@@ -300,48 +300,58 @@ __device__ __forceinline__ uint64_t page_rec(uint32_t row, uint32_t nn, uint32_t
 
 // Gathers the tile's locators through the row ids into `ol` (read back by the
 // later passes in output order), and packs the tile: its page count, and for
-// a prefix-summed tile its page starts.
+// a prefix-summed tile its page starts.  Thread t takes the tile's rows
+// 8t .. 8t+7 from the start: its row ids as two 16-byte loads, its eight
+// locator gathers in flight together, its locators kept in registers for the
+// packing and stored to `ol` as 16-byte writes (no shared-memory staging).
 __global__ void __launch_bounds__(kPackT) k_pack_count(PackCols P, uint64_t ntiles) {
     __shared__ uint32_t sm[33];
     __shared__ uint64_t s_scan[33];
-    __shared__ uint64_t s_loc[kStrTile];  // the tile's locators in row order
+    __shared__ uint64_t s_last[kPackT / 32];  // each warp's last locator
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (uint64_t g = blockIdx.x; g < ntiles; g += gridDim.x) {
         const PackCol& v  = P.c[pack_col_of(P, g)];
         const uint64_t t  = g - v.tile_base;
         const uint64_t t0 = t * kStrTile, t1 = (v.n < t0 + kStrTile ? v.n : t0 + kStrTile);
         const uint32_t nt = uint32_t(t1 - t0);
-        // gather with coalesced row ids (rows k * kPackT + thread): all row ids
-        // first, then all locators, then the stores in output order
+        const uint32_t li0  = threadIdx.x * kPackRow;  // this thread's first row in the tile
+        const uint64_t r0   = t0 + li0;
+        const uint32_t rows = li0 >= nt ? 0u : (nt - li0 < kPackRow ? nt - li0 : uint32_t(kPackRow));
+        const bool     full = rows == kPackRow;
+        uint64_t       loc[kPackRow];
         {
             uint32_t src[kPackRow];
-            uint64_t lg[kPackRow];
+            if (v.rid && full && (reinterpret_cast<uintptr_t>(v.rid + r0) & 15) == 0) {
+                const uint4 x = __ldg(reinterpret_cast<const uint4*>(v.rid + r0));
+                const uint4 y = __ldg(reinterpret_cast<const uint4*>(v.rid + r0) + 1);
+                src[0] = x.x; src[1] = x.y; src[2] = x.z; src[3] = x.w;
+                src[4] = y.x; src[5] = y.y; src[6] = y.z; src[7] = y.w;
+            } else {
 #pragma unroll
-            for (int k = 0; k < kPackRow; ++k) {
-                const uint32_t li = uint32_t(k) * kPackT + threadIdx.x;
-                src[k]            = li < nt ? (v.rid ? __ldg(v.rid + t0 + li) : uint32_t(t0 + li)) : 0u;
+                for (int k = 0; k < kPackRow; ++k) src[k] = v.rid && uint32_t(k) < rows ? __ldg(v.rid + r0 + k) : 0u;
             }
 #pragma unroll
-            for (int k = 0; k < kPackRow; ++k) {
-                const uint32_t li = uint32_t(k) * kPackT + threadIdx.x;
-                lg[k]             = li < nt ? __ldg(v.locs + (v.rid ? uint64_t(src[k]) : t0 + li)) : 0ull;
-            }
+            for (int k = 0; k < kPackRow; ++k)
+                loc[k] = uint32_t(k) < rows ? __ldg(v.locs + (v.rid ? uint64_t(src[k]) : r0 + k)) : 0ull;
+            if (full && (reinterpret_cast<uintptr_t>(v.ol + r0) & 15) == 0) {
+                ulonglong2* o = reinterpret_cast<ulonglong2*>(v.ol + r0);
 #pragma unroll
-            for (int k = 0; k < kPackRow; ++k) {
-                const uint32_t li = uint32_t(k) * kPackT + threadIdx.x;
-                if (li < nt) v.ol[t0 + li] = lg[k];
-                s_loc[li] = lg[k];
+                for (int k = 0; k < kPackRow; k += 2) o[k / 2] = make_ulonglong2(loc[k], loc[k + 1]);
+            } else {
+#pragma unroll
+                for (int k = 0; k < kPackRow; ++k)
+                    if (uint32_t(k) < rows) v.ol[r0 + k] = loc[k];
             }
         }
-        __syncthreads();
-        // packing: thread t takes the tile's rows t * kPackRow .. + kPackRow - 1
-        const uint64_t r0 = t0 + uint64_t(threadIdx.x) * kPackRow;
-        const uint32_t rows = r0 >= t1 ? 0u : (t1 - r0 < kPackRow ? uint32_t(t1 - r0) : uint32_t(kPackRow));
+        // the locator of the row before this thread's first: the previous
+        // lane's last, or across warps through shared memory (read after the
+        // barriers of tile_max_any)
+        uint64_t prev = __shfl_up_sync(0xffffffffu, loc[kPackRow - 1], 1);
+        if (lane == 31) s_last[warp] = loc[kPackRow - 1];
         uint64_t*      rec  = v.recs + t * kRec;
-        uint64_t       loc[kPackRow];
-#pragma unroll
-        for (int k = 0; k < kPackRow; ++k) loc[k] = s_loc[threadIdx.x * kPackRow + k];  // 0 past the tile's rows
         TileCosts c = row_costs(loc, rows);
         tile_max_any(c.maxc, c.greedy, sm);
+        if (lane == 0 && warp > 0) prev = s_last[warp - 1];
         if (c.greedy) {
             if (threadIdx.x < 32) {
                 const uint32_t np = pack_tile(v.ol, v.base, v.npages, t0, t1, nullptr);
@@ -358,11 +368,10 @@ __global__ void __launch_bounds__(kPackT) k_pack_count(PackCols P, uint64_t ntil
         // exclusive prefix of (non-NULL rows << 40 | string bytes) at this thread's first row
         uint64_t       tot;
         const uint64_t pre = block_exclusive_scan<uint64_t>((uint64_t(c.nn) << 40) | c.len, s_scan, &tot);
-        const uint32_t li0 = uint32_t(r0 - t0);
         uint32_t       NN = uint32_t(pre >> 40), LEN = uint32_t(pre & ((1ull << 40) - 1));
         // S: the row's start in eighths of a byte (offsets, string bytes, one bit per row)
         uint32_t S       = 8u * (2u * NN + LEN) + li0;
-        uint32_t pg_prev = li0 > 0 && rows > 0 ? (S - loc_cost(s_loc[li0 - 1])) / T : 0u;
+        uint32_t pg_prev = li0 > 0 && rows > 0 ? (S - loc_cost(prev)) / T : 0u;
 #pragma unroll
         for (int k = 0; k < kPackRow; ++k) {
             if (uint32_t(k) >= rows) break;
@@ -464,54 +473,83 @@ __device__ __forceinline__ void copy_string(uint8_t* img, uint32_t dst, const ui
     }
 }
 
-// One warp per output page, assembled in the warp's own 8 KB of shared memory
-// (no block barriers): 32-row chunks, a warp scan of (non-NULL, bytes) per
-// chunk, one string per lane, then the image is stored with 16-byte writes.
-constexpr int kVW = 8;  // warps (pages in flight) per block
+// One output page per kVWP warps, assembled in one 8 KB image in shared
+// memory: the page's 32-row chunks are split into kVWP contiguous parts, one
+// per warp (a part's first rank and byte come from summing the locators before
+// it), each warp runs a warp scan of (non-NULL, bytes) per chunk with one
+// string per lane, and the image is stored with 16-byte writes.  The warps of
+// a page meet only at two named barriers per page (image zeroed; image
+// complete); a page's latency chain of dependent string loads is split
+// kVWP ways without more shared memory, which keeps L1 for the string loads.
+constexpr int kVWP  = 2;  // warps per page
+constexpr int kVPB  = 4;  // pages in flight per block
+constexpr int kVMin = 4;  // blocks per SM
+constexpr int kVT   = kVWP * kVPB * 32;
+static_assert(kVPB <= 15, "one named barrier per page slot");
 
-__global__ void __launch_bounds__(kVW * 32)
+// Barrier of the kVWP warps of page slot `slot` (named barrier 1 + slot; the
+// warp is reconverged first, as bar.sync requires).
+__device__ __forceinline__ void page_sync(unsigned slot) {
+    __syncwarp();
+    if (kVWP > 1) asm volatile("bar.sync %0, %1;" ::"r"(1 + slot), "r"(32 * kVWP) : "memory");
+}
+
+__global__ void __launch_bounds__(kVT, kVMin)
     k_write_varchar_pages(const PageDesc* __restrict__ desc, uint64_t ndesc, const uint64_t* __restrict__ ol,
                           const uint8_t* __restrict__ base, uint64_t npages, uint8_t* __restrict__ out) {
     extern __shared__ __align__(16) uint8_t vimg[];
     const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint8_t*       img  = vimg + size_t(warp) * kPage;
-    uint4*         w4   = reinterpret_cast<uint4*>(img);
-    for (uint64_t pi = uint64_t(blockIdx.x) * kVW + warp; pi < ndesc; pi += uint64_t(gridDim.x) * kVW) {
+    const unsigned slot = warp / kVWP, part = warp % kVWP;
+    uint8_t*       img  = vimg + size_t(slot) * kPage;
+    constexpr int  kQ   = kPage / 16 / (32 * kVWP);  // 16-byte words per lane of a part's share
+    uint4*         w4   = reinterpret_cast<uint4*>(img) + part * 32 * kQ;  // this part's share of the image
+    for (uint64_t pi = uint64_t(blockIdx.x) * kVPB + slot; pi < ndesc; pi += uint64_t(gridDim.x) * kVPB) {
         const PageDesc d = desc[pi];
 #pragma unroll
-        for (int k = 0; k < kPage / 16 / 32; ++k) w4[lane + 32 * k] = make_uint4(0, 0, 0, 0);
-        __syncwarp();
+        for (int k = 0; k < kQ; ++k) w4[lane + 32 * k] = make_uint4(0, 0, 0, 0);
+        page_sync(slot);  // strings may cross into the other parts' shares
         if (d.count == 0) {  // long-string page `chunk` of the string in row d.row
-            const uint64_t loc = ol[d.row];
-            const uint32_t L   = loc_len(loc, base, npages);
-            const uint32_t beg = d.chunk * kLongChunk;
-            const uint32_t len = min(kLongChunk, L - beg);
-            if (lane == 0) {
-                *reinterpret_cast<uint16_t*>(img)     = d.chunk == 0 ? 0xffff : 0xfffe;
-                *reinterpret_cast<uint16_t*>(img + 2) = uint16_t(len);
-            }
-            // source: the 0xffff page and its 0xfffe continuations, in order
-            uint64_t q  = loc_off(loc) / kPage;
-            uint32_t so = 0;  // string offset of page q's first byte
-            for (; q < npages && so < beg + len; ++q) {
-                const uint8_t* pg = base + q * kPage;
-                const uint32_t pl = *reinterpret_cast<const uint16_t*>(pg + 2);
-                const uint32_t lo = max(so, beg), hi = min(so + pl, beg + len);
-                for (uint32_t x = lo + lane; x < hi; x += 32) img[4 + x - beg] = pg[4 + x - so];
-                so += pl;
+            if (part == 0) {
+                const uint64_t loc = ol[d.row];
+                const uint32_t L   = loc_len(loc, base, npages);
+                const uint32_t beg = d.chunk * kLongChunk;
+                const uint32_t len = min(kLongChunk, L - beg);
+                if (lane == 0) {
+                    *reinterpret_cast<uint16_t*>(img)     = d.chunk == 0 ? 0xffff : 0xfffe;
+                    *reinterpret_cast<uint16_t*>(img + 2) = uint16_t(len);
+                }
+                // source: the 0xffff page and its 0xfffe continuations, in order
+                uint64_t q  = loc_off(loc) / kPage;
+                uint32_t so = 0;  // string offset of page q's first byte
+                for (; q < npages && so < beg + len; ++q) {
+                    const uint8_t* pg = base + q * kPage;
+                    const uint32_t pl = *reinterpret_cast<const uint16_t*>(pg + 2);
+                    const uint32_t lo = max(so, beg), hi = min(so + pl, beg + len);
+                    for (uint32_t x = lo + lane; x < hi; x += 32) img[4 + x - beg] = pg[4 + x - so];
+                    so += pl;
+                }
             }
         } else {
             const uint32_t data0  = 4 + 2 * d.nn;
             const uint32_t nbytes = (d.count + 7) / 8, bm0 = kPage - nbytes;
-            uint32_t       rank0 = 0, byte0 = 0;
-            uint64_t       next  = lane < d.count ? ol[d.row + lane] : 0;
-            for (uint32_t c = 0; c < d.count; c += 32) {
+            // this part's rows: whole 32-row chunks, so parts own disjoint bitmap bytes
+            const uint32_t nch = (d.count + 31) / 32, per = (nch + kVWP - 1) / kVWP;
+            const uint32_t r0  = min(d.count, part * per * 32), r1 = min(d.count, (part + 1) * per * 32);
+            // (non-NULL count << 16 | bytes) before the part: a page holds at
+            // most 4094 non-NULL rows and 8188 string bytes, so the halves never carry
+            uint32_t pre = 0;
+            for (uint32_t r = lane; r < r0 && r0 < r1; r += 32) {
+                const uint64_t loc = ol[d.row + r];
+                pre += loc != 0 ? 0x10000u | uint32_t(loc_len_field(loc)) : 0u;
+            }
+            pre            = warp_sum(pre);
+            uint32_t rank0 = pre >> 16, byte0 = pre & 0xffffu;
+            uint64_t next  = r0 + lane < r1 ? ol[d.row + r0 + lane] : 0;
+            for (uint32_t c = r0; c < r1; c += 32) {
                 const uint64_t loc = next;
-                next               = c + 32 + lane < d.count ? ol[d.row + c + 32 + lane] : 0;
+                next               = c + 32 + lane < r1 ? ol[d.row + c + 32 + lane] : 0;
                 const bool     on  = loc != 0;
                 const uint32_t len = on ? uint32_t(loc_len_field(loc)) : 0u;
-                // (non-NULL count << 16 | bytes): a page holds at most 8188 string
-                // bytes, so the low half never carries into the high one
                 const uint32_t v    = (on ? 0x10000u : 0u) | len;
                 const uint32_t inc  = warp_inclusive_scan<uint32_t>(v);
                 const uint32_t tot  = __shfl_sync(0xffffffffu, inc, 31);
@@ -529,16 +567,17 @@ __global__ void __launch_bounds__(kVW * 32)
                 rank0 += tot >> 16;
                 byte0 += tot & 0xffffu;
             }
-            if (lane == 0) {
+            if (part == 0 && lane == 0) {
                 *reinterpret_cast<uint16_t*>(img)     = uint16_t(d.count);
                 *reinterpret_cast<uint16_t*>(img + 2) = uint16_t(d.nn);
             }
         }
-        __syncwarp();
-        uint4* dst = reinterpret_cast<uint4*>(out + pi * kPage);
+        page_sync(slot);  // image complete
+        // each part stores its own share; the next page zeroes only that
+        // share, and its first barrier orders the other parts' writes after
+        uint4* dst = reinterpret_cast<uint4*>(out + pi * kPage) + part * 32 * kQ;
 #pragma unroll
-        for (int k = 0; k < kPage / 16 / 32; ++k) dst[lane + 32 * k] = w4[lane + 32 * k];
-        __syncwarp();
+        for (int k = 0; k < kQ; ++k) dst[lane + 32 * k] = w4[lane + 32 * k];
     }
 }
 
@@ -609,8 +648,8 @@ std::vector<uint8_t*> varchar_write(std::vector<VarcharOut*>& vs, const std::vec
         if (v.n == 0) continue;
         out[i] = static_cast<uint8_t*>(dalloc(std::max<uint64_t>(pages[i], 1) * kPage, st));
         HJ_CUDA(cudaFuncSetAttribute(k_write_varchar_pages, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     kVW * kPage));
-        k_write_varchar_pages<<<grid_of(div_up(pages[i], kVW), 3), kVW * 32, kVW * kPage, st>>>(
+                                     kVPB * kPage));
+        k_write_varchar_pages<<<grid_of(div_up(pages[i], kVPB), kVMin), kVT, kVPB * kPage, st>>>(
             v.desc, pages[i], v.ol, v.base, v.base_pages, out[i]);
         HJ_LAUNCH_CHECK();
         for (void* p : {(void*)v.desc, (void*)v.ol, (void*)v.tile_pages, (void*)v.tile_off, (void*)v.recs})
