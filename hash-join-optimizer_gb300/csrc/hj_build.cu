@@ -326,7 +326,6 @@ __global__ void __launch_bounds__(1024)
     const uint32_t part = blockIdx.x;
     const uint32_t nl   = 1u << g.L;
     const uint64_t gb   = uint64_t(part) << g.L;
-    const uint32_t P    = 1u << g.R;
     uint32_t       run  = part_off[part];
     if (fused_part(part_off, part)) return;  // k_bucket_local (also writes the sentinel word)
     if (part_off[part + 1] == run) {  // empty partition: all buckets empty
@@ -594,22 +593,23 @@ __global__ void __launch_bounds__(kThreads)
     bool     single;
     if (!chunk_range(blockIdx.x, chunk_off, chunk_part, part_off, 1u << g.R, part, s, e, single)) return;
     if (fused_part(part_off, part)) return;  // set by k_bucket_local
-    // four tuples per thread at a time: keys, then directory words, then first keys
-    for (uint32_t j0 = s + threadIdx.x; j0 < e; j0 += 4 * blockDim.x) {
-        int32_t  k[4];
-        uint64_t p[4], first[4];
+    // kMU tuples per thread at a time: keys, then directory words, then first keys
+    constexpr int kMU = 8;
+    for (uint32_t j0 = s + threadIdx.x; j0 < e; j0 += kMU * blockDim.x) {
+        int32_t  k[kMU];
+        uint32_t p[kMU], first[kMU];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int u = 0; u < kMU; ++u) {
             const uint32_t j = j0 + u * blockDim.x;
             k[u]             = j < e ? key[j] : 0;
         }
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            p[u]     = bucket_of(fib_hash(k[u]), g.b);
-            first[u] = j0 + u * blockDim.x < e ? __ldg(dir + p[u]) >> 16 : 0;
+        for (int u = 0; u < kMU; ++u) {
+            p[u]     = uint32_t(bucket_of(fib_hash(k[u]), g.b));
+            first[u] = j0 + u * blockDim.x < e ? uint32_t(__ldg(dir + p[u]) >> 16) : 0u;
         }
 #pragma unroll
-        for (int u = 0; u < 4; ++u)
+        for (int u = 0; u < kMU; ++u)
             if (j0 + u * blockDim.x < e && key[first[u]] != k[u]) atomicOr(mixed + (p[u] >> 5), 1u << (p[u] & 31));
     }
 }

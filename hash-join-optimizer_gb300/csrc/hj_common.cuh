@@ -115,7 +115,11 @@ __device__ __forceinline__ bool int_get(const IntCol& c, uint64_t r, int32_t& v)
         v = __ldg(c.plain + r);
         return bit_valid(c.valid, r);
     }
-    const uint64_t p = r / uint64_t(kDenseRows);
+    // page of row r: a 32-bit division by the constant for rows below 2^32
+    // (every column the engine reads), the 64-bit one above
+    uint64_t p;
+    if ((r >> 32) == 0) p = uint32_t(r) / uint32_t(kDenseRows);
+    else                p = r / uint64_t(kDenseRows);
     v = __ldg(reinterpret_cast<const int32_t*>(c.pages + p * kPage + 4) + (r - p * uint64_t(kDenseRows)));
     return true;
 }
