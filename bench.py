@@ -18,6 +18,10 @@ build, probe, and the output written as reference-format pages.
          same inputs, all host threads (the whole workload when it takes at
          most about 30 s of CPU time, else a stated probe-side prefix)
 
+The default c2 line also carries `workloads` (c1 and c3 at full size, device
+time and probe roofline of each) and `systems` (the batched and served forms
+at reduced size, each against the plain path).
+
 The inputs (>2 GB of pages) exceed the 126 MB L2, so no flush is needed
 between steps.  `--impl reference` times the CPU restatement alone, one
 execute() of the same workload per step, with input pages built by the
@@ -70,6 +74,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-systems", action="store_true",
                     help="c2: leave out the batched and served summaries (c4 / c5 at reduced size)")
+    ap.add_argument("--no-workloads", action="store_true",
+                    help="c2: leave out the c1 and c3 summaries (full size, 100 steps each)")
     ap.add_argument("--e2e-depth", type=int, default=3,
                     help="plans in flight in the pipelined end-to-end mode (1 = serial only)")
     ap.add_argument("--e2e-pageable", action="store_true",
@@ -650,6 +656,28 @@ def systems_summary(args, d: Dist) -> dict:
     }
 
 
+def workloads_summary(args, d: Dist) -> dict:
+    """The two other plain-path configurations at full size, attached to the
+    default c2 line (one GPU) so that a plain `python bench.py` records them
+    too: c1 (1M x 10M unique keys) and c3 (the 5-relation chain), each with
+    device-resident inputs, 100 timed steps, its phase times and the probe
+    roofline.  `--workload c1|c3` runs either with every leg (e2e, CPU
+    baseline)."""
+    import copy
+    out = {}
+    for name in ("c1", "c3"):
+        a = copy.copy(args)
+        a.workload, a.scale, a.steps, a.warmup = name, 1.0, 100, 3
+        a.no_e2e, a.no_cpu_baseline = True, True
+        r = run_ours(a, d)
+        out[name] = {"workload": r["config"]["workload"], "steps": r["steps"], "ms_per_step": r["ms_per_step"],
+                     "probe_tuples_per_s": r["value"], "build_tuples_per_s": r["build_tuples_per_s"],
+                     "output_rows": r["config"]["output_rows"], "phases_ms": r["phases_ms"],
+                     "probe_roofline_frac": r["roofline"]["frac"], "probe_achieved_gbs": r["roofline"]["achieved"],
+                     "algorithmic_bytes": r["roofline"]["algorithmic_bytes"], "gpu_launches": r["gpu_launches"]}
+    return out
+
+
 def main():
     args = parse()
     d = Dist()
@@ -661,6 +689,9 @@ def main():
         line = run_serve(args, d)
     else:
         line = run_ours(args, d)
+        if (line is not None and args.workload == "c2" and args.scale == 1.0 and d.world == 1
+                and not args.no_workloads):
+            line["workloads"] = workloads_summary(args, d)
         if (line is not None and args.workload == "c2" and args.scale == 1.0 and d.world == 1
                 and not args.no_systems):
             line["systems"] = systems_summary(args, d)
