@@ -309,9 +309,23 @@ __global__ void __launch_bounds__(kPT, 2)
             }
         }
         __syncthreads();
-        // global ranges first (hist still holds the counts), then local offsets
-        for (uint32_t k = threadIdx.x; k < np2; k += kPT)
-            if (hist[k]) gbase[k] = off[s.part_base + k] + atomicAdd(fill + s.part_base + k, hist[k]);
+        // global ranges first (hist still holds the counts), then local offsets;
+        // a thread's reservations four at a time, all four in flight before
+        // any result is stored
+        for (uint32_t k0 = threadIdx.x; k0 < np2; k0 += 4 * kPT) {
+            uint64_t g[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const uint32_t k = k0 + uint32_t(u) * kPT;
+                const uint32_t c = k < np2 ? hist[k] : 0u;
+                g[u]             = c ? off[s.part_base + k] + atomicAdd(fill + s.part_base + k, c) : 0ull;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const uint32_t k = k0 + uint32_t(u) * kPT;
+                if (k < np2 && hist[k]) gbase[k] = g[u];
+            }
+        }
         for (uint32_t k = threadIdx.x; k < np2; k += kPT) loff[k] = hist[k];
         __syncthreads();
         smem_scan(loff, np2, false, wsum);
