@@ -58,17 +58,21 @@ int num_sms() {
 
 // ---------------------------------------------------------------- memory ----
 
-// Large blocks (result pages, decoded columns, row-id streams: >= 64 MB) are
-// kept per stream when freed on the stream that allocated them, and handed
-// back to the next allocation of a similar size on that stream without going
-// through the pool: stream order makes the reuse safe, and the host never
-// waits on the pool's memory mapping between two kernels.  A block freed on
-// another stream (a served result, freed through the server's context) goes
-// back to the pool, and a stream keeps at most kKeepPerStream bytes.
-// flush_stream() returns a stream's blocks.
+// Blocks are kept per stream when freed on the stream that allocated them,
+// and handed back to the next allocation of a similar size on that stream
+// without going through the pool: stream order makes the reuse safe, the host
+// never waits on the pool's memory mapping between two kernels, and the
+// dozens of small temporaries of an execute (counters, offsets, page
+// descriptors) cost no driver call.  Large blocks (result pages, decoded
+// columns, row-id streams: >= 64 MB) are sized in 16 MB granules and reused
+// up to 25% larger; smaller ones in power-of-two classes from 4 KB, reused
+// from their own class.  A block freed on another stream (a served result,
+// freed through the server's context) goes back to the pool, and a stream
+// keeps at most kKeepPerStream bytes.  flush_stream() returns a stream's blocks.
 namespace {
 constexpr size_t kBig           = size_t(64) << 20;
 constexpr size_t kGranule       = size_t(16) << 20;
+constexpr size_t kSmallMin      = size_t(4) << 10;
 constexpr size_t kKeepPerStream = size_t(48) << 30;
 struct BigBlock {
     size_t       bytes;
@@ -109,39 +113,39 @@ void flush_stream(cudaStream_t st) {
 }
 
 void* dalloc(size_t bytes, cudaStream_t st) {
-    if (bytes == 0) bytes = 16;
     if (bytes >= kBig) {
         bytes = (bytes + kGranule - 1) / kGranule * kGranule;
-        BigBlocks& b = big_blocks();
-        {
-            std::lock_guard<std::mutex> g(b.mu);
-            auto&                       m  = b.free[st];
-            auto                        it = m.lower_bound(bytes);
-            if (it != m.end() && it->first <= bytes + bytes / 4) {
-                void* p = it->second;
-                b.kept[st] -= it->first;
-                m.erase(it);
-                return p;
-            }
-        }
-        void* p = pool_alloc(bytes, st);
-        if (!p) {  // give every cached block back and try once more
-            std::vector<cudaStream_t> streams;
-            {
-                std::lock_guard<std::mutex> g(b.mu);
-                for (auto& kv : b.free) streams.push_back(kv.first);
-            }
-            for (auto s2 : streams) flush_stream(s2);
-            cudaDeviceSynchronize();
-            p = pool_alloc(bytes, st);
-        }
-        if (!p) throw Error(HJ_ERR_NOMEM, "device allocation of " + std::to_string(bytes) + " bytes failed");
+    } else {
+        size_t c = kSmallMin;
+        while (c < bytes) c <<= 1;
+        bytes = c;
+    }
+    BigBlocks& b = big_blocks();
+    {
         std::lock_guard<std::mutex> g(b.mu);
-        b.size[p] = BigBlock{bytes, st};
-        return p;
+        auto&                       m  = b.free[st];
+        auto                        it = m.lower_bound(bytes);
+        if (it != m.end() && it->first <= bytes + bytes / 4) {
+            void* p = it->second;
+            b.kept[st] -= it->first;
+            m.erase(it);
+            return p;
+        }
     }
     void* p = pool_alloc(bytes, st);
+    if (!p) {  // give every cached block back and try once more
+        std::vector<cudaStream_t> streams;
+        {
+            std::lock_guard<std::mutex> g(b.mu);
+            for (auto& kv : b.free) streams.push_back(kv.first);
+        }
+        for (auto s2 : streams) flush_stream(s2);
+        cudaDeviceSynchronize();
+        p = pool_alloc(bytes, st);
+    }
     if (!p) throw Error(HJ_ERR_NOMEM, "device allocation of " + std::to_string(bytes) + " bytes failed");
+    std::lock_guard<std::mutex> g(b.mu);
+    b.size[p] = BigBlock{bytes, st};
     return p;
 }
 
