@@ -321,6 +321,11 @@ struct BuiltKey {
 // from it (hj_server); every access holds `mu`.
 struct Store {
     std::mutex                                  mu;
+    // Host -> HBM uploads of the contexts that share this store (a server's
+    // slots) run one plan at a time: two plans uploading at once only split
+    // the host link's upload direction, and they slow the result downloads of
+    // finished plans that share the link.
+    std::mutex                                  upload_mu;
     std::map<uint64_t, std::shared_ptr<DevTable>> tables;
     std::map<BuiltKey, std::shared_ptr<Table>>    built;
     uint64_t                                    next_handle = 1;
@@ -1270,6 +1275,12 @@ int hj_execute(hj_context* c, const hj_plan_desc* plan, hj_result** out) {
                 if (n.filters[f].column < t.num_columns) want[n.base_table_id][n.filters[f].column] = true;
         }
         ex.phase("upload");
+        // the store's upload turn, held while this plan's host tables are copied
+        // (upload_table returns once its copies are complete)
+        std::unique_lock<std::mutex> upload_turn(c->store->upload_mu, std::defer_lock);
+        bool host_inputs = false;
+        for (uint32_t i = 0; i < plan->num_inputs; ++i) host_inputs |= plan->inputs[i].resident == 0;
+        if (host_inputs) upload_turn.lock();
         for (uint32_t i = 0; i < plan->num_inputs; ++i) {
             const hj_table_desc& t = plan->inputs[i];
             if (t.resident) {
@@ -1288,6 +1299,7 @@ int hj_execute(hj_context* c, const hj_plan_desc* plan, hj_result** out) {
                 ex.tables.push_back(hj::upload_table(c, t, want[i]));
             }
         }
+        if (host_inputs) upload_turn.unlock();
         // copy_scan of every scanned column, before any join (execute.cpp:575-582)
         ex.phase("decode");
         for (uint32_t i = 0; i < plan->num_nodes; ++i) {
