@@ -13,11 +13,14 @@
 // adjacency array on the host with per-thread slab buffers
 // (include/slab_allocator.h) and three phases.  Here the slabs are replaced by
 // a two-level MSD radix partition:
-//   1. k_part_hist      histogram of the top R hash bits (R = b - 13)
+//   1. k_part_hist      histogram of the top R hash bits (R = b - 12)
 //   2. k_part_offsets   partition offsets and per-partition chunk counts
 //   3. k_part_scatter   (key, row) pairs scattered to their partition
+// Partitions of at most kFuseMax tuples are then built by one block each
+// (k_bucket_local); the larger ones (Zipf-heavy keys) take steps 4-7, with
+// their counters cleared first (k_bucket_zero):
 //   4. k_bucket_count   per 8192-tuple chunk: shared-memory bucket counts and
-//                       Bloom tags over the partition's 2^13 buckets
+//                       Bloom tags over the partition's 2^12 buckets
 //   5. k_bucket_dir     per partition: prefix sum -> directory words
 //   6. k_bucket_scatter per chunk: tuples to their final adjacency slots
 //   7. k_bucket_mixed   flags buckets that hold more than one distinct key
