@@ -60,7 +60,8 @@ def test_seeded_small_workloads_match_reference_checksums(engine, orc):
         assert (n, counts, str(cks)) == (g["num_rows"], g["column_rows"], g["checksum"]), name
 
 
-@pytest.mark.parametrize("name,scale", [("c1", 1.0), ("c2", 1 / 16), ("c3", 0.1), ("c3", 1.0), ("c2", 0.01)])
+@pytest.mark.parametrize("name,scale", [("c1", 1.0), ("c2", 1 / 16), ("c3", 0.1), ("c3", 1.0), ("c2", 0.01),
+                                        ("c2", 1.0)])
 def test_workloads_match_oracle(engine, orc, name, scale):
     from hjgb300 import workloads
     w = getattr(workloads, name)(scale=scale)
@@ -322,6 +323,52 @@ def test_table_probe_pairs(engine, hj, orc):
         assert np.array_equal(np.bincount(pr, minlength=probe.size - 1), want_u)
     finally:
         L.hj_table_free(t)
+
+
+def test_large_skewed_builds_match_unchained_hash(engine, hj, orc):
+    """Builds of 2^21 keys whose partitions exceed one block's shared memory
+    (Zipf-heavy keys, and 150 keys of 13,000 tuples, several sharing a
+    partition): the same directory words as UnchainedHash, and every probe
+    match found."""
+    import ctypes as C
+    import torch
+    L = hj.lib()
+    r = np.random.default_rng(11)
+    n = 1 << 21
+    zipf = r.permutation(np.arange(1 << 19, dtype=np.int64))[(r.zipf(1.15, n) - 1) % (1 << 19)].astype(np.int32)
+    zipf[:4] = [2**31 - 1, -(2**31), -7, 0]
+    heavy = r.choice(np.arange(-(1 << 29), 1 << 29, dtype=np.int64), 150, replace=False).astype(np.int32)
+    flat = np.concatenate([np.repeat(heavy, 13_000),
+                           r.integers(-(1 << 30), 1 << 30, n - 1_950_000).astype(np.int32)])
+    flat = flat[r.permutation(n)]
+    for build in (zipf, flat):
+        # every distinct build key once (n matches in all), and keys that miss
+        probe = np.concatenate([r.permutation(np.unique(build)),
+                                r.integers(1 << 20, 1 << 21, 100_000).astype(np.int32) | (1 << 30)])
+        want_dir = orc.unchained_directory(build)
+        want = orc.unchained_counts(build, probe)
+        kb, kp = torch.from_numpy(build).cuda(), torch.from_numpy(probe).cuda()
+        t = C.c_void_p()
+        assert L.hj_table_build(engine.handle, kb.data_ptr(), None, kb.numel(), -1, C.byref(t)) == 0
+        try:
+            bits, nt, d = C.c_uint32(), C.c_uint64(), C.c_void_p()
+            L.hj_table_info(t, C.byref(bits), C.byref(nt), C.byref(d), None, None)
+            assert nt.value == n
+            dev = torch.as_tensor(_Dev(d.value, (1 << bits.value) + 1, "<u8"), device="cuda").cpu().numpy()
+            assert np.array_equal(dev.astype(np.uint64), want_dir.astype(np.uint64))
+            nm = C.c_uint64()
+            rc = L.hj_table_probe(engine.handle, t, kp.data_ptr(), None, kp.numel(), None, None, 0, C.byref(nm))
+            assert rc == hj.HJ_ERR_CAPACITY and nm.value == int(want.sum())
+            op = torch.empty(nm.value, dtype=torch.int32, device="cuda")
+            ob = torch.empty(nm.value, dtype=torch.int32, device="cuda")
+            assert L.hj_table_probe(engine.handle, t, kp.data_ptr(), None, kp.numel(), op.data_ptr(),
+                                    ob.data_ptr(), nm.value, C.byref(nm)) == 0
+            pr, br = op.cpu().numpy(), ob.cpu().numpy()
+            assert np.array_equal(probe[pr], build[br])
+            assert np.array_equal(np.bincount(pr, minlength=probe.size), want)
+            assert np.unique(pr.astype(np.int64) << 32 | br).size == pr.size
+        finally:
+            L.hj_table_free(t)
 
 
 def _varchar_pages_fit(pages):
