@@ -203,9 +203,19 @@ __device__ __forceinline__ void smem_scan(uint32_t* a, uint32_t n, bool inclusiv
     __syncthreads();
 }
 
+// 0. the relation of every partition-pass item, so that the histogram and
+// scatter blocks find an item's relation with one load instead of a binary
+// search of dependent loads each
+__global__ void k_item_rel(const RelInst* __restrict__ R, uint32_t nr, uint64_t items, uint32_t* __restrict__ rmap) {
+    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    for (uint64_t t = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; t < items; t += stride)
+        rmap[t] = owner(nr, t, [&](uint32_t i) { return R[i].item_base; });
+}
+
 // 1. per (relation, partition) row counts
 __global__ void __launch_bounds__(kPT)
-    k_bpart_hist(const RelInst* __restrict__ R, uint32_t nr, uint64_t items, uint32_t* __restrict__ cnt) {
+    k_bpart_hist(const RelInst* __restrict__ R, const uint32_t* __restrict__ rmap, uint64_t items,
+                 uint32_t* __restrict__ cnt) {
     // Items of equal size go to the blocks round robin (no queue, no barrier
     // per item).  The block's counts accumulate in shared memory over its items
     // of one relation and go to global memory when the relation changes (items
@@ -219,7 +229,7 @@ __global__ void __launch_bounds__(kPT)
             if (hist[k]) atomicAdd(cnt + c.part_base + k, hist[k]);
     };
     for (uint64_t t = blockIdx.x; t < items; t += gridDim.x) {
-        const uint32_t ri = owner(nr, t, [&](uint32_t i) { return R[i].item_base; });
+        const uint32_t ri = __ldg(rmap + t);
         const RelInst& s  = R[ri];
         const uint64_t r0 = (t - s.item_base) * kPartItem;
         const uint64_t r1 = min(s.rows, r0 + kPartItem);
@@ -265,7 +275,8 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // partition with each one's row in the item, then per partition its count,
 // its first sorted row and its global base.
 __global__ void __launch_bounds__(kPT, 2)
-    k_bpart_scatter(const RelInst* __restrict__ R, uint32_t nr, uint64_t items, unsigned long long* q,
+    k_bpart_scatter(const RelInst* __restrict__ R, const uint32_t* __restrict__ rmap, uint64_t items,
+                    unsigned long long* q,
                     const uint64_t* __restrict__ off, uint32_t* __restrict__ fill, uint32_t pmax,
                     int32_t* __restrict__ okey, int32_t* __restrict__ opay) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -280,7 +291,7 @@ __global__ void __launch_bounds__(kPT, 2)
     constexpr int kPer = kPartItem / kPT;
     static_assert(kPartItem <= 65536, "row in the item fits 16 bits");
     for (uint64_t t = next_item(q, &sh); t < items; t = next_item(q, &sh)) {
-        const RelInst& s  = R[owner(nr, t, [&](uint32_t i) { return R[i].item_base; })];
+        const RelInst& s  = R[__ldg(rmap + t)];
         const uint64_t r0 = (t - s.item_base) * kPartItem;
         const uint64_t r1 = min(s.rows, r0 + kPartItem);
         if (r0 >= r1) continue;
@@ -384,6 +395,19 @@ __global__ void k_bjoin_plan(const InstInfo* __restrict__ I, uint32_t n, uint64_
     }
 }
 
+// 4b. the (instance partition, instance) of every join work item, written by
+// each instance partition for its items (one load per item in the join)
+__global__ void k_bjoin_map(const InstInfo* __restrict__ I, uint32_t n, uint64_t nip, const uint64_t* __restrict__ joff,
+                            uint2* __restrict__ jmap) {
+    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    for (uint64_t e = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < nip; e += stride) {
+        const uint64_t a = joff[e], b = joff[e + 1];
+        if (a == b) continue;
+        const uint32_t ii = owner(n, e, [&](uint32_t i) { return I[i].ip_base; });
+        for (uint64_t t = a; t < b; ++t) jmap[t] = make_uint2(uint32_t(e), ii);
+    }
+}
+
 // 5. join.  Shared memory: the build rows of the item's partition in every
 // build relation (keys, payloads; at most `cap` rows together), then per
 // table its bucket bounds.  Table j (relation j + 1) has 2^bits_j buckets
@@ -394,8 +418,8 @@ __global__ void k_bjoin_plan(const InstInfo* __restrict__ I, uint32_t n, uint64_
 // and forms fingerprints only for complete matches; duplicate keys are
 // enumerated by an odometer over the match lists.
 __global__ void __launch_bounds__(kPT, 2)
-    k_bjoin(const InstInfo* __restrict__ I, uint32_t n, uint64_t nip, const uint64_t* __restrict__ joff,
-            unsigned long long* q, const uint64_t* __restrict__ off, const int32_t* __restrict__ key,
+    k_bjoin(const InstInfo* __restrict__ I, const uint2* __restrict__ jmap, uint64_t nip,
+            const uint64_t* __restrict__ joff, unsigned long long* q, const uint64_t* __restrict__ off, const int32_t* __restrict__ key,
             const int32_t* __restrict__ pay, uint32_t cap, uint32_t scap, uint32_t max_bits, uint32_t load_q8,
             unsigned long long* __restrict__ rows, unsigned long long* __restrict__ sums, uint32_t* __restrict__ ovf) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -410,8 +434,8 @@ __global__ void __launch_bounds__(kPT, 2)
     __shared__ uint64_t g_src[kMaxRel];
     const uint64_t items = joff[nip];
     for (uint64_t t = next_item(q, &sh); t < items; t = next_item(q, &sh)) {
-        const uint32_t  e   = owner(uint32_t(nip), t, [&](uint32_t i) { return joff[i]; });
-        const uint32_t  ii  = owner(n, e, [&](uint32_t i) { return I[i].ip_base; });
+        const uint2     em  = jmap[t];
+        const uint32_t  e   = em.x, ii = em.y;
         const InstInfo& s   = I[ii];
         const uint32_t  pb  = s.pbits;
         const uint32_t  nt  = s.nrel - 1;  // tables
@@ -671,7 +695,7 @@ std::vector<uint32_t> batch_execute(const std::vector<BatchInstance>& B, const B
 
     std::vector<RelInst>  hr;
     std::vector<InstInfo> hi(n);
-    uint64_t pbase = 0, ipbase = 0, items = 0, total_rows = 0;
+    uint64_t pbase = 0, ipbase = 0, items = 0, total_rows = 0, r0_rows = 0;
     uint32_t pmax = 0;
     for (uint32_t i = 0; i < n; ++i) {
         uint64_t nb = 0;
@@ -689,6 +713,7 @@ std::vector<uint32_t> batch_execute(const std::vector<BatchInstance>& B, const B
             items += (br.rows + kPartItem - 1) / kPartItem;
             total_rows += br.rows;
         }
+        r0_rows += B[i].rels[0].rows;
         pbase += uint64_t(s.nrel) << p;
         ipbase += 1ull << p;
     }
@@ -721,6 +746,9 @@ std::vector<uint32_t> batch_execute(const std::vector<BatchInstance>& B, const B
     auto* tmp    = static_cast<uint64_t*>(take((std::max(scan_tmp_words(pbase), scan_tmp_words(ipbase)) + 1) * 8));
     auto* pkey   = static_cast<int32_t*>(take(total_rows * 4));
     auto* ppay   = static_cast<int32_t*>(take(total_rows * 4));
+    auto* rmap   = static_cast<uint32_t*>(take(items * 4));
+    // join items: at most one per instance partition plus one per kJoinChunk R0 rows
+    auto* jmap   = static_cast<uint2*>(take((ipbase + r0_rows / kJoinChunk + 1) * 8));
     HJ_CUDA(cudaMemcpyAsync(d_R, hr.data(), nr * sizeof(RelInst), cudaMemcpyHostToDevice, st));
     HJ_CUDA(cudaMemcpyAsync(d_I, hi.data(), n * sizeof(InstInfo), cudaMemcpyHostToDevice, st));
     HJ_CUDA(cudaStreamSynchronize(st));  // the host arrays stay alive until here
@@ -741,22 +769,28 @@ std::vector<uint32_t> batch_execute(const std::vector<BatchInstance>& B, const B
         HJ_CUDA(cudaMemsetAsync(cnt, 0, (pbase + 1) * 4, st));
         HJ_CUDA(cudaMemsetAsync(fill, 0, (pbase + 1) * 4, st));
         if (items) {
-            k_bpart_hist<<<grid_for(g_hist, items), kPT, hist_smem, st>>>(d_R, nr, items, cnt);
+            k_item_rel<<<unsigned(std::min<uint64_t>(div_up(items, 256), uint64_t(num_sms()) * 8)), 256, 0, st>>>(
+                d_R, nr, items, rmap);
+            HJ_LAUNCH_CHECK();
+            k_bpart_hist<<<grid_for(g_hist, items), kPT, hist_smem, st>>>(d_R, rmap, items, cnt);
             HJ_LAUNCH_CHECK();
         }
         scan_exclusive_u32_to_u64_into(cnt, off, pbase, tmp, st);
         if (items) {
-            k_bpart_scatter<<<grid_for(g_scat, items), kPT, scat_smem, st>>>(d_R, nr, items, d_q + 1, off, fill, pmax,
-                                                                             pkey, ppay);
+            k_bpart_scatter<<<grid_for(g_scat, items), kPT, scat_smem, st>>>(d_R, rmap, items, d_q + 1, off, fill,
+                                                                             pmax, pkey, ppay);
             HJ_LAUNCH_CHECK();
         }
         k_bjoin_plan<<<unsigned(std::min<uint64_t>(div_up(ipbase, 256), uint64_t(num_sms()) * 8)), 256, 0, st>>>(
             d_I, n, ipbase, off, jcnt);
         HJ_LAUNCH_CHECK();
         scan_exclusive_u32_to_u64_into(jcnt, joff, ipbase, tmp, st);
+        k_bjoin_map<<<unsigned(std::min<uint64_t>(div_up(ipbase, 256), uint64_t(num_sms()) * 8)), 256, 0, st>>>(
+            d_I, n, ipbase, joff, jmap);
+        HJ_LAUNCH_CHECK();
         // the item count lives on the device: launch the resident grid
-        k_bjoin<<<unsigned(g_join), kPT, join_smem, st>>>(d_I, n, ipbase, joff, d_q + 2, off, pkey, ppay, cap, scap,
-                                                          max_bits, load_q8, d_rows, d_sums, d_ovf);
+        k_bjoin<<<unsigned(g_join), kPT, join_smem, st>>>(d_I, jmap, ipbase, joff, d_q + 2, off, pkey, ppay, cap,
+                                                          scap, max_bits, load_q8, d_rows, d_sums, d_ovf);
         HJ_LAUNCH_CHECK();
     };
     if (o.graph) {
