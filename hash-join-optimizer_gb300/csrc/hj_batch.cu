@@ -416,11 +416,13 @@ __global__ void k_bjoin_map(const InstInfo* __restrict__ I, uint32_t n, uint64_t
 // Each R0 row looks its key up in every table (a cheap compare loop that
 // notes the first match and the count), stops at the first table without it,
 // and forms fingerprints only for complete matches; duplicate keys are
-// enumerated by an odometer over the match lists.
+// enumerated by an odometer over the match lists.  In chains of three or more
+// relations the rows that pass table 0 are queued per warp and looked up in
+// the later tables 32 at a time.
 __global__ void __launch_bounds__(kPT, 2)
     k_bjoin(const InstInfo* __restrict__ I, const uint2* __restrict__ jmap, uint64_t nip,
-            const uint64_t* __restrict__ joff, unsigned long long* q, const uint64_t* __restrict__ off, const int32_t* __restrict__ key,
-            const int32_t* __restrict__ pay, uint32_t cap, uint32_t scap, uint32_t max_bits, uint32_t load_q8,
+            const uint64_t* __restrict__ joff, unsigned long long* q, const uint64_t* __restrict__ off,
+            const int32_t* __restrict__ key, const int32_t* __restrict__ pay, uint32_t cap, uint32_t scap, uint32_t max_bits, uint32_t load_q8,
             unsigned long long* __restrict__ rows, unsigned long long* __restrict__ sums, uint32_t* __restrict__ ovf) {
     extern __shared__ __align__(16) unsigned char smem[];
     int32_t*  skey = reinterpret_cast<int32_t*>(smem);
@@ -432,6 +434,11 @@ __global__ void __launch_bounds__(kPT, 2)
     // table geometry of the current item: bits, rows, first S word, source offset
     __shared__ uint32_t g_tb[kMaxRel], g_tn[kMaxRel], g_ts[kMaxRel], g_words, g_nb, g_skip;
     __shared__ uint64_t g_src[kMaxRel];
+    // per warp: rows that matched table 0 once, waiting for the later tables
+    constexpr uint32_t  kRing = 64;
+    __shared__ int32_t  ring_key[kPT / 32][kRing];
+    __shared__ uint64_t ring_fp[kPT / 32][kRing];
+    const uint32_t      lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint64_t items = joff[nip];
     for (uint64_t t = next_item(q, &sh); t < items; t = next_item(q, &sh)) {
         const uint2     em  = jmap[t];
@@ -526,54 +533,27 @@ __global__ void __launch_bounds__(kPT, 2)
         const int32_t* pk = key + x0;
         const int32_t* pp = pay + x0;
         unsigned long long my_rows = 0, my_sum = 0;
-        // the next row's key and payload are loaded while this row is looked up
-        int32_t k_next = threadIdx.x < m ? __ldg(pk + threadIdx.x) : 0;
-        int32_t p_next = threadIdx.x < m ? __ldg(pp + threadIdx.x) : 0;
-        for (uint32_t x = threadIdx.x; x < m; x += kPT) {
-            const int32_t k = k_next, pv = p_next;
-            if (x + kPT < m) {
-                k_next = __ldg(pk + x + kPT);
-                p_next = __ldg(pp + x + kPT);
-            }
-            uint32_t      cj[kMaxRel];  // matches << 16 | first match (tables hold < 2^16 rows)
-            bool          all = true, dup = false;
-#pragma unroll
-            for (uint32_t j = 0; j < kMaxRel; ++j) {
-                if (j >= nt) break;
-                const uint32_t b  = g_ts[j] + bucket(j, k);
-                const uint32_t be = S[b + 2];
-                uint32_t       cnt = 0, j1 = 0;
-                for (uint32_t y = S[b + 1]; y < be; ++y)
-                    if (skey[y] == k) {
-                        j1 = cnt ? j1 : y;
-                        ++cnt;
-                    }
-                cj[j] = (cnt << 16) | j1;
-                dup |= cnt > 1;
-                if (!cnt) {
-                    all = false;
-                    break;
+        // matches of key k in table j: their count, and the first in `first`
+        auto lookup = [&](uint32_t j, int32_t k, uint32_t& first) {
+            const uint32_t b  = g_ts[j] + bucket(j, k);
+            const uint32_t be = S[b + 2];
+            uint32_t       cnt = 0, j1 = 0;
+            for (uint32_t y = S[b + 1]; y < be; ++y)
+                if (skey[y] == k) {
+                    j1 = cnt ? j1 : y;
+                    ++cnt;
                 }
-            }
-            if (!all) continue;
-            uint64_t fp = fp_start(k, pv);
-            if (!dup) {
-#pragma unroll
-                for (uint32_t j = 0; j < kMaxRel; ++j) {
-                    if (j >= nt) break;
-                    fp = fp_add(fp, spay[cj[j] & 0xffffu]);
-                }
-                ++my_rows;
-                my_sum += fp_final(fp);
-                continue;
-            }
-            // duplicates: every combination of one match per table (odometer)
+            first = j1;
+            return cnt;
+        };
+        // every combination of one match per table j0 .. nt-1 for key k, the
+        // tables before j0 folded into fp (an odometer over the match lists)
+        auto enumerate = [&](uint32_t j0, int32_t k, uint64_t fp) {
             uint32_t first[kMaxRel], pos[kMaxRel];
             uint64_t fpl[kMaxRel + 1];
-#pragma unroll
-            for (uint32_t j = 0; j < kMaxRel; ++j) first[j] = j < nt ? (cj[j] & 0xffffu) : 0u;
-            fpl[0] = fp;
-            for (uint32_t j = 0; j < nt; ++j) {
+            fpl[j0] = fp;
+            for (uint32_t j = j0; j < nt; ++j) {
+                if (!lookup(j, k, first[j])) return;
                 pos[j]     = first[j];
                 fpl[j + 1] = fp_add(fpl[j], spay[pos[j]]);
             }
@@ -581,7 +561,7 @@ __global__ void __launch_bounds__(kPT, 2)
                 ++my_rows;
                 my_sum += fp_final(fpl[nt]);
                 int j = int(nt) - 1;
-                for (; j >= 0; --j) {
+                for (; j >= int(j0); --j) {
                     const uint32_t be = S[g_ts[j] + bucket(uint32_t(j), k) + 2];
                     uint32_t       y  = pos[j] + 1;
                     while (y < be && skey[y] != k) ++y;
@@ -591,9 +571,79 @@ __global__ void __launch_bounds__(kPT, 2)
                     }
                     pos[j] = first[j];
                 }
-                if (j < 0) break;
+                if (j < int(j0)) break;
                 for (uint32_t z = uint32_t(j); z < nt; ++z) fpl[z + 1] = fp_add(fpl[z], spay[pos[z]]);
             }
+        };
+        // the next row's key and payload are loaded while this row is looked up
+        int32_t k_next = threadIdx.x < m ? __ldg(pk + threadIdx.x) : 0;
+        int32_t p_next = threadIdx.x < m ? __ldg(pp + threadIdx.x) : 0;
+        if (nt == 1) {
+            for (uint32_t x = threadIdx.x; x < m; x += kPT) {
+                const int32_t k = k_next, pv = p_next;
+                if (x + kPT < m) {
+                    k_next = __ldg(pk + x + kPT);
+                    p_next = __ldg(pp + x + kPT);
+                }
+                uint32_t       f;
+                const uint32_t c = lookup(0, k, f);
+                if (c == 1) {
+                    ++my_rows;
+                    my_sum += fp_final(fp_add(fp_start(k, pv), spay[f]));
+                } else if (c > 1) {
+                    enumerate(0, k, fp_start(k, pv));
+                }
+            }
+        } else {
+            // Table 0 is looked up for every row.  Rows with one match there
+            // queue up in the warp's ring (key and fold state) and the later
+            // tables are looked up 32 queued rows at a time, so that lanes
+            // whose row missed table 0 do not idle through them.
+            int32_t*       qk   = ring_key[warp];
+            uint64_t*      qf   = ring_fp[warp];
+            uint32_t       qh = 0, qt = 0;  // ring head and tail (warp-uniform)
+            auto drain = [&](uint32_t cnt) {
+                __syncwarp();
+                if (lane < cnt) {
+                    const uint32_t slot = (qh + lane) % kRing;
+                    const int32_t  k    = qk[slot];
+                    uint64_t       fp   = qf[slot];
+                    uint32_t       j = 1, c = 1;
+                    for (; j < nt; ++j) {
+                        uint32_t f;
+                        c = lookup(j, k, f);
+                        if (c != 1) break;
+                        fp = fp_add(fp, spay[f]);
+                    }
+                    if (j == nt) {
+                        ++my_rows;
+                        my_sum += fp_final(fp);
+                    } else if (c > 1) {
+                        enumerate(j, k, fp);
+                    }
+                }
+                qh += cnt;
+                __syncwarp();
+            };
+            for (uint32_t x = threadIdx.x; x - lane < m; x += kPT) {  // warp-uniform bound
+                const int32_t k = k_next, pv = p_next;
+                if (x + kPT < m) {
+                    k_next = __ldg(pk + x + kPT);
+                    p_next = __ldg(pp + x + kPT);
+                }
+                uint32_t f = 0, c = 0;
+                if (x < m) c = lookup(0, k, f);
+                if (c > 1) enumerate(0, k, fp_start(k, pv));
+                const unsigned hm = __ballot_sync(0xffffffffu, c == 1);
+                if (c == 1) {
+                    const uint32_t slot = (qt + __popc(hm & ((1u << lane) - 1u))) % kRing;
+                    qk[slot]            = k;
+                    qf[slot]            = fp_add(fp_start(k, pv), spay[f]);
+                }
+                qt += __popc(hm);
+                if (qt - qh >= 32) drain(32);
+            }
+            drain(qt - qh);
         }
         unsigned long long tr, tsum;
         block_exclusive_scan<unsigned long long>(my_rows, red, &tr);

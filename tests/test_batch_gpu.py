@@ -141,6 +141,50 @@ def test_batch_duplicates_empty_and_mixed_depths(engine, hj):
         engine.set_option("batch_part_log2", saved)
 
 
+def test_batch_deep_chains_with_duplicates(engine, hj):
+    """Chains of 3 to 8 relations with tens of thousands of probe rows: the
+    rows that pass the first table are queued per warp for the later ones, so
+    the queue fills, wraps and drains many times; duplicate keys in the first,
+    a middle and the last table go through the odometer from each position."""
+    import torch
+    r = np.random.default_rng(17)
+    dom = 4000
+
+    def build(n, dup_frac):
+        k = r.choice(dom, n, replace=False)
+        d = r.choice(k, int(n * dup_frac), replace=False)
+        k = np.concatenate([k, d, d[: d.size // 3]])
+        return r.permutation(k), r.integers(-2**31, 2**31 - 1, k.size)
+
+    host = []
+    for m, dups in ((3, {1}), (3, set()), (4, {2}), (5, {4}), (6, {1, 3}), (8, set()), (8, {7})):
+        rels = [(r.integers(0, dom, 40_000), r.integers(-2**31, 2**31 - 1, 40_000))]
+        for j in range(1, m):
+            rels.append(build(3000, 0.05 if j in dups else 0.0))
+        host.append([(k.astype(np.int32), v.astype(np.int32)) for k, v in rels])
+    keep, insts = [], []
+    for inst in host:
+        rels = []
+        for k, v in inst:
+            tk, tv = torch.from_numpy(k).cuda(), torch.from_numpy(v).cuda()
+            keep += [tk, tv]
+            rels.append((tk.data_ptr(), tv.data_ptr(), k.size))
+        insts.append(rels)
+    torch.cuda.synchronize()
+    want = [bo.chain_result(inst) for inst in host]
+    assert all(w[0] > 1000 for w in want)
+    saved = engine.get_option("batch_part_log2")
+    try:
+        for mode, part in ((hj.BATCH_PERSISTENT, 12), (hj.BATCH_PERSISTENT, 9), (hj.BATCH_PLAIN, 12)):
+            engine.set_option("batch_part_log2", part)
+            rows, sums, redo = engine.batch_execute(insts, mode)
+            assert [(int(a), int(b)) for a, b in zip(rows, sums)] == want, (mode, part)
+            if mode == hj.BATCH_PERSISTENT:
+                assert redo == 0
+    finally:
+        engine.set_option("batch_part_log2", saved)
+
+
 def test_batch_rejects_bad_instances(engine, hj):
     import torch
     k = torch.zeros(4, dtype=torch.int32, device="cuda")
