@@ -109,7 +109,7 @@ __global__ void k_batch_generate(uint64_t seed, uint32_t inst, uint32_t rel, uin
 //   3. rows into partition order                             k_bpart_scatter
 //      (block-local counting sort in shared memory, payloads staged by
 //      cp.async meanwhile, one global range reservation per (block,
-//      partition), runs written out coalesced)
+//      partition), runs written out coalesced as (key, payload) pairs)
 //   4. join work list: (instance partition, chunk of its R0 rows)
 //                                                            k_bjoin_plan
 //   5. per work item: the partition of every build relation becomes a
@@ -278,7 +278,7 @@ __global__ void __launch_bounds__(kPT, 2)
     k_bpart_scatter(const RelInst* __restrict__ R, const uint32_t* __restrict__ rmap, uint64_t items,
                     unsigned long long* q,
                     const uint64_t* __restrict__ off, uint32_t* __restrict__ fill, uint32_t pmax,
-                    int32_t* __restrict__ okey, int32_t* __restrict__ opay) {
+                    int2* __restrict__ okp) {
     extern __shared__ __align__(16) unsigned char smem[];
     int32_t*  spay  = reinterpret_cast<int32_t*>(smem);   // row order
     int32_t*  skey  = spay + kPartItem;                    // partition order
@@ -356,8 +356,7 @@ __global__ void __launch_bounds__(kPT, 2)
             const int32_t  k   = skey[j];
             const uint32_t p   = part_of(k, pb);
             const uint64_t pos = gbase[p] + (j - loff[p]);
-            okey[pos]          = k;
-            opay[pos]          = spay[sidx[j]];
+            okp[pos]           = make_int2(k, spay[sidx[j]]);
         }
         __syncthreads();  // the next item overwrites spay
     }
@@ -422,7 +421,7 @@ __global__ void k_bjoin_map(const InstInfo* __restrict__ I, uint32_t n, uint64_t
 __global__ void __launch_bounds__(kPT, 2)
     k_bjoin(const InstInfo* __restrict__ I, const uint2* __restrict__ jmap, uint64_t nip,
             const uint64_t* __restrict__ joff, unsigned long long* q, const uint64_t* __restrict__ off,
-            const int32_t* __restrict__ key, const int32_t* __restrict__ pay, uint32_t cap, uint32_t scap, uint32_t max_bits, uint32_t load_q8,
+            const int2* __restrict__ kp, uint32_t cap, uint32_t scap, uint32_t max_bits, uint32_t load_q8,
             unsigned long long* __restrict__ rows, unsigned long long* __restrict__ sums, uint32_t* __restrict__ ovf) {
     extern __shared__ __align__(16) unsigned char smem[];
     int32_t*  skey = reinterpret_cast<int32_t*>(smem);
@@ -491,11 +490,11 @@ __global__ void __launch_bounds__(kPT, 2)
         constexpr uint32_t kBU = 4;
         for (uint32_t j = 0; j < nt; ++j) {
             const uint32_t tn = g_tn[j];
-            const int32_t* kj = key + g_src[j];
+            const int32_t* kj = reinterpret_cast<const int32_t*>(kp + g_src[j]);  // keys: even words
             for (uint32_t r = threadIdx.x; r < tn; r += kBU * kPT) {
                 int32_t kk[kBU];
 #pragma unroll
-                for (uint32_t u = 0; u < kBU; ++u) kk[u] = r + u * kPT < tn ? __ldg(kj + r + u * kPT) : 0;
+                for (uint32_t u = 0; u < kBU; ++u) kk[u] = r + u * kPT < tn ? __ldg(kj + 2 * (r + u * kPT)) : 0;
 #pragma unroll
                 for (uint32_t u = 0; u < kBU; ++u)
                     if (r + u * kPT < tn) atomicAdd(&S[g_ts[j] + bucket(j, kk[u]) + 1], 1u);
@@ -505,15 +504,14 @@ __global__ void __launch_bounds__(kPT, 2)
         smem_scan(S, words, true, wsum);
         for (uint32_t j = 0; j < nt; ++j) {
             const uint32_t tn = g_tn[j];
-            const int32_t* kj = key + g_src[j];
-            const int32_t* pj = pay + g_src[j];
+            const int2* qj = kp + g_src[j];
             for (uint32_t r = threadIdx.x; r < tn; r += kBU * kPT) {
                 int32_t kk[kBU], pv[kBU];
 #pragma unroll
                 for (uint32_t u = 0; u < kBU; ++u) {
-                    const bool in = r + u * kPT < tn;
-                    kk[u]         = in ? __ldg(kj + r + u * kPT) : 0;
-                    pv[u]         = in ? __ldg(pj + r + u * kPT) : 0;
+                    const int2 v = r + u * kPT < tn ? __ldg(qj + r + u * kPT) : make_int2(0, 0);
+                    kk[u]        = v.x;
+                    pv[u]        = v.y;
                 }
 #pragma unroll
                 for (uint32_t u = 0; u < kBU; ++u)
@@ -530,12 +528,10 @@ __global__ void __launch_bounds__(kPT, 2)
         const uint64_t cs = join_chunk(g_nb);
         const uint64_t x0 = p0 + (t - joff[e]) * cs;
         const uint32_t m  = uint32_t(min(p0 + part_rows(off, s.part_base + l), x0 + cs) - x0);
-        const int32_t* pk = key + x0;
-        const int32_t* pp = pay + x0;
+        const int2*    pq = kp + x0;
         unsigned long long my_rows = 0, my_sum = 0;
-        // matches of key k in table j: their count, and the first in `first`
-        auto lookup = [&](uint32_t j, int32_t k, uint32_t& first) {
-            const uint32_t b  = g_ts[j] + bucket(j, k);
+        // matches of key k in bucket word b: their count, and the first in `first`
+        auto scan_bucket = [&](uint32_t b, int32_t k, uint32_t& first) {
             const uint32_t be = S[b + 2];
             uint32_t       cnt = 0, j1 = 0;
             for (uint32_t y = S[b + 1]; y < be; ++y)
@@ -545,6 +541,14 @@ __global__ void __launch_bounds__(kPT, 2)
                 }
             first = j1;
             return cnt;
+        };
+        auto lookup = [&](uint32_t j, int32_t k, uint32_t& first) {
+            return scan_bucket(g_ts[j] + bucket(j, k), k, first);
+        };
+        // table 0, which every row meets, with its geometry in registers
+        const uint32_t ts0 = g_ts[0], sh0 = 32 - g_tb[0];
+        auto lookup0 = [&](int32_t k, uint32_t& first) {
+            return scan_bucket(ts0 + ((fib_hi(k) << pb) >> sh0), k, first);
         };
         // every combination of one match per table j0 .. nt-1 for key k, the
         // tables before j0 folded into fp (an odometer over the match lists)
@@ -576,17 +580,13 @@ __global__ void __launch_bounds__(kPT, 2)
             }
         };
         // the next row's key and payload are loaded while this row is looked up
-        int32_t k_next = threadIdx.x < m ? __ldg(pk + threadIdx.x) : 0;
-        int32_t p_next = threadIdx.x < m ? __ldg(pp + threadIdx.x) : 0;
+        int2 q_next = threadIdx.x < m ? __ldg(pq + threadIdx.x) : make_int2(0, 0);
         if (nt == 1) {
             for (uint32_t x = threadIdx.x; x < m; x += kPT) {
-                const int32_t k = k_next, pv = p_next;
-                if (x + kPT < m) {
-                    k_next = __ldg(pk + x + kPT);
-                    p_next = __ldg(pp + x + kPT);
-                }
+                const int32_t k = q_next.x, pv = q_next.y;
+                if (x + kPT < m) q_next = __ldg(pq + x + kPT);
                 uint32_t       f;
-                const uint32_t c = lookup(0, k, f);
+                const uint32_t c = lookup0(k, f);
                 if (c == 1) {
                     ++my_rows;
                     my_sum += fp_final(fp_add(fp_start(k, pv), spay[f]));
@@ -626,13 +626,10 @@ __global__ void __launch_bounds__(kPT, 2)
                 __syncwarp();
             };
             for (uint32_t x = threadIdx.x; x - lane < m; x += kPT) {  // warp-uniform bound
-                const int32_t k = k_next, pv = p_next;
-                if (x + kPT < m) {
-                    k_next = __ldg(pk + x + kPT);
-                    p_next = __ldg(pp + x + kPT);
-                }
+                const int32_t k = q_next.x, pv = q_next.y;
+                if (x + kPT < m) q_next = __ldg(pq + x + kPT);
                 uint32_t f = 0, c = 0;
-                if (x < m) c = lookup(0, k, f);
+                if (x < m) c = lookup0(k, f);
                 if (c > 1) enumerate(0, k, fp_start(k, pv));
                 const unsigned hm = __ballot_sync(0xffffffffu, c == 1);
                 if (c == 1) {
@@ -794,8 +791,7 @@ std::vector<uint32_t> batch_execute(const std::vector<BatchInstance>& B, const B
     auto* jcnt   = static_cast<uint32_t*>(take((ipbase + 1) * 4));
     auto* joff   = static_cast<uint64_t*>(take((ipbase + 2) * 8));
     auto* tmp    = static_cast<uint64_t*>(take((std::max(scan_tmp_words(pbase), scan_tmp_words(ipbase)) + 1) * 8));
-    auto* pkey   = static_cast<int32_t*>(take(total_rows * 4));
-    auto* ppay   = static_cast<int32_t*>(take(total_rows * 4));
+    auto* pkp    = static_cast<int2*>(take(total_rows * 8));  // (key, payload) in partition order
     auto* rmap   = static_cast<uint32_t*>(take(items * 4));
     // join items: at most one per instance partition plus one per kJoinChunk R0 rows
     auto* jmap   = static_cast<uint2*>(take((ipbase + r0_rows / kJoinChunk + 1) * 8));
@@ -828,7 +824,7 @@ std::vector<uint32_t> batch_execute(const std::vector<BatchInstance>& B, const B
         scan_exclusive_u32_to_u64_into(cnt, off, pbase, tmp, st);
         if (items) {
             k_bpart_scatter<<<grid_for(g_scat, items), kPT, scat_smem, st>>>(d_R, rmap, items, d_q + 1, off, fill,
-                                                                             pmax, pkey, ppay);
+                                                                             pmax, pkp);
             HJ_LAUNCH_CHECK();
         }
         k_bjoin_plan<<<unsigned(std::min<uint64_t>(div_up(ipbase, 256), uint64_t(num_sms()) * 8)), 256, 0, st>>>(
@@ -839,7 +835,7 @@ std::vector<uint32_t> batch_execute(const std::vector<BatchInstance>& B, const B
             d_I, n, ipbase, joff, jmap);
         HJ_LAUNCH_CHECK();
         // the item count lives on the device: launch the resident grid
-        k_bjoin<<<unsigned(g_join), kPT, join_smem, st>>>(d_I, jmap, ipbase, joff, d_q + 2, off, pkey, ppay, cap,
+        k_bjoin<<<unsigned(g_join), kPT, join_smem, st>>>(d_I, jmap, ipbase, joff, d_q + 2, off, pkp, cap,
                                                           scap, max_bits, load_q8, d_rows, d_sums, d_ovf);
         HJ_LAUNCH_CHECK();
     };
