@@ -255,7 +255,8 @@ def run_e2e(args, d: Dist, hj, eng, w, npr: int, out_pages: list, stream) -> dic
                and the result download of a third overlap (the link carries
                both directions at once for page-locked memory).
     Both modes are reported (`modes`); `value` is the faster one, named in
-    `mode`."""
+    `mode`.  Each mode's time is a median over timed blocks, leaving out blocks
+    that a busy host link slowed (see `timed`)."""
     import ctypes as C
     import collections
     import numpy as np
@@ -278,7 +279,7 @@ def run_e2e(args, d: Dist, hj, eng, w, npr: int, out_pages: list, stream) -> dic
             locked.append(a)
     h2d = sum(a.nbytes for a in inputs)
     d2h_seen = []
-    parts = {"upload_ms": 0.0, "execute_ms": 0.0, "fetch_ms": 0.0}
+    step_parts = []  # per serial step: upload, execute and fetch ms
 
     def fetch(r):
         total = 0
@@ -298,11 +299,9 @@ def run_e2e(args, d: Dist, hj, eng, w, npr: int, out_pages: list, stream) -> dic
         t0 = time.perf_counter()
         r = eng.execute_raw(host_plan)
         t1 = time.perf_counter()
-        ph = eng.stats(r)[3]
-        parts["upload_ms"] += ph.get("upload", 0.0)
-        parts["execute_ms"] += 1e3 * (t1 - t0) - ph.get("upload", 0.0)
+        up = eng.stats(r)[3].get("upload", 0.0)
         fetch(r)
-        parts["fetch_ms"] += 1e3 * (time.perf_counter() - t1)
+        step_parts.append((up, 1e3 * (t1 - t0) - up, 1e3 * (time.perf_counter() - t1)))
         eng.free_result(r)
 
     # the host link's bandwidth right before each timed block: a 512 MiB
@@ -322,35 +321,53 @@ def run_e2e(args, d: Dist, hj, eng, w, npr: int, out_pages: list, stream) -> dic
             out.append(round(src.numel() * 2 / (a.elapsed_time(b) * 1e6), 1))
         return out
 
-    def timed(fn, k, blocks=5, links=None):
-        """Median over `blocks` timed blocks of k steps: the host link is shared
-        with the machine's other GPUs, whose traffic shows up as outlier blocks
-        (`links` collects the link probe taken before each block)."""
+    all_links = []  # every link probe of the run, both modes
+
+    def timed(fn, k, blocks=9, links=None):
+        """Median over `blocks` timed blocks of k steps.  The host link is
+        shared with the machine's other GPUs, whose traffic shows up as slow
+        blocks; `links` collects the link probe taken before each block (the
+        lowest over ranks).  Blocks whose probe found either direction below
+        80% of the best probe so far in this run (either mode) are left out of
+        the median when at least three blocks remain; otherwise every block
+        counts.  Returns the median,
+        every block's time and the indices of the blocks in the median."""
         per = []
         for _ in range(blocks):
             d.barrier()
             torch.cuda.synchronize()
             if links is not None:
-                links.append(link_gbs())
+                links.append([-d.max(-x) for x in link_gbs()])
+                all_links.append(links[-1])
             s2, e2 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             s2.record(stream)
             fn(k)
             e2.record(stream)
             torch.cuda.synchronize()
             per.append(d.max(s2.elapsed_time(e2) / k))
-        return sorted(per)[len(per) // 2], per
+        used = list(range(len(per)))
+        if links:
+            best = [max(x[i] for x in all_links) for i in (0, 1)]
+            quiet = [b for b, x in enumerate(links) if all(x[i] >= 0.8 * best[i] for i in (0, 1))]
+            if len(quiet) >= 3:
+                used = quiet
+        sel = sorted(per[b] for b in used)
+        return sel[len(sel) // 2], per, used
 
     k2 = max(1, min(args.steps, 5))
     try:
         serial_step()
-        for key in parts:
-            parts[key] = 0.0
+        step_parts.clear()
         d2h_seen.clear()
         serial_links = []
-        serial_ms, serial_blocks = timed(lambda k: [serial_step() for _ in range(k)], k2, links=serial_links)
+        serial_ms, serial_blocks, serial_used = timed(lambda k: [serial_step() for _ in range(k)], k2,
+                                                      links=serial_links)
+        # steps of the blocks in the median (block b holds steps b*k2 .. b*k2+k2-1)
+        kept = [p for i, p in enumerate(step_parts) if i // k2 in serial_used]
         modes = {"serial": {"ms_per_step": serial_ms, "blocks_ms_per_step": [round(x, 3) for x in serial_blocks],
-                            "link_gbs_h2d_d2h_before_block": serial_links,
-                            "parts_ms": {key: round(v / (len(serial_blocks) * k2), 3) for key, v in parts.items()}}}
+                            "link_gbs_h2d_d2h_before_block": serial_links, "blocks_in_median": serial_used,
+                            "parts_ms": {key: round(sum(p[i] for p in kept) / max(1, len(kept)), 3)
+                                         for i, key in enumerate(("upload_ms", "execute_ms", "fetch_ms"))}}}
         out = {"value": npr * d.world / (serial_ms / 1e3), "unit": "probe tuples/s", "ms_per_step": serial_ms,
                "mode": "serial", "host_memory": "pageable" if args.e2e_pageable else "page-locked",
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": int(sum(d2h_seen) / max(1, len(d2h_seen))),
@@ -387,12 +404,12 @@ def run_e2e(args, d: Dist, hj, eng, w, npr: int, out_pages: list, stream) -> dic
                 for v in seen.values():
                     v.clear()
                 pipe_links = []
-                pipe_ms, pipe_blocks = timed(pipelined, kp, links=pipe_links)
+                pipe_ms, pipe_blocks, pipe_used = timed(pipelined, kp, links=pipe_links)
             finally:
                 srv.close()
             modes["pipelined"] = {"ms_per_step": pipe_ms, "plans_in_flight": depth,
                                   "blocks_ms_per_step": [round(x, 3) for x in pipe_blocks],
-                                  "link_gbs_h2d_d2h_before_block": pipe_links,
+                                  "link_gbs_h2d_d2h_before_block": pipe_links, "blocks_in_median": pipe_used,
                                   "median_per_plan_ms": {k: round(sorted(v)[len(v) // 2], 3)
                                                          for k, v in seen.items() if v}}
             if pipe_ms < serial_ms:
