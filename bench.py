@@ -537,6 +537,53 @@ def run_ours(args, d: Dist) -> dict:
     }
 
 
+def chain_plan(hj, rels):
+    """A c4 instance [(keys, payload), ...] as the left-deep plan the
+    reference would run: R0 joins R1 on the key, the result joins R2, ...;
+    output key, p0, ..., pm-1 (INT32)."""
+    p = hj.Plan()
+    for k, v in rels:
+        p.new_input(hj.Table(k.size, [hj.Column.int32(k), hj.Column.int32(v)]))
+    scans = [p.new_scan_node(j, [(0, hj.INT32), (1, hj.INT32)]) for j in range(len(rels))]
+    cur, width = scans[0], 2
+    for j in range(1, len(rels)):
+        attrs = [(c, hj.INT32) for c in range(width)] + [(width + 1, hj.INT32)]
+        cur = p.new_join_node(False, cur, scans[j], 0, 0, attrs)
+        width += 1
+    p.root = cur
+    return p
+
+
+def c4_cpu_sample(hj, w, gpu_rows, budget_s: float, n: int = 64) -> dict:
+    """CPU baseline of c4: a seeded sample of n instances, each one run as its
+    left-deep plan through the oracle's restatement of execute() with all host
+    threads (relations from the oracle's generator, paged untimed), in sample
+    order until the sample is done or budget_s of execute() time is spent.
+    Each instance's row count is checked against the GPU's."""
+    import numpy as np
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import batch_oracle as bo
+    oracle = oracle_mod()
+    threads = os.cpu_count() or 1
+    os.environ["SIGMOD_THREADS"] = str(threads)
+    pick = np.random.default_rng(4096).choice(len(w), min(n, len(w)), replace=False)
+    secs, done, probe, same = 0.0, 0, 0, True
+    for i in pick:
+        iid, m, b, q, pr = w.instance(int(i))
+        plan = chain_plan(hj, bo.instance_relations(w.seed, iid, m, b, q, pr))
+        st = oracle.timed_execute(plan)
+        secs += st["seconds"]
+        done += 1
+        probe += pr
+        same &= st["rows"] == int(gpu_rows[int(i)])
+        if secs > budget_s:
+            break
+    return {"value": done / secs, "unit": "queries/s", "cores": threads, "kind": "port",
+            "sample": f"{done} of a seeded {len(pick)}-instance sample ({probe} probe rows), each a left-deep plan "
+                      f"through the restated execute() to finished result pages; {secs:.1f} s of execute()",
+            "rows_equal_gpu": bool(same)}
+
+
 def run_batch(args, d: Dist) -> dict:
     """c4: the batched form against the plain one-query-at-a-time path."""
     import numpy as np
@@ -584,6 +631,9 @@ def run_batch(args, d: Dist) -> dict:
     t_plain = d.max(t_plain)
     same = bool(np.array_equal(prow, rows[:npl]) and np.array_equal(psum, sums[:npl]))
     eng.close()
+    cpu = None
+    if d.rank == 0 and not args.no_cpu_baseline:
+        cpu = c4_cpu_sample(hj, w, rows, args.cpu_budget_s)
     q_batch = len(w) * d.world / t_batch
     q_plain = npl * d.world / t_plain
     probe_rows = int(w.probe_rows.sum())
@@ -601,7 +651,7 @@ def run_batch(args, d: Dist) -> dict:
                              "plain": {k: v for k, v in tuned["plain"].items() if k != "seconds"}}},
         "plain": {"value": q_plain, "unit": "queries/s", "instances": npl, "seconds": t_plain},
         "speedup_vs_plain": q_batch / q_plain, "results_equal_plain": same, "recomputed": redo,
-        "probe_tuples_per_s": probe_rows / t_batch, "clocks": clocks,
+        "probe_tuples_per_s": probe_rows / t_batch, "cpu_baseline": cpu, "clocks": clocks,
     }
 
 
@@ -717,21 +767,23 @@ def workloads_summary(args, d: Dist) -> dict:
     """The two other plain-path configurations at full size, attached to the
     default c2 line (one GPU) so that a plain `python bench.py` records them
     too: c1 (1M x 10M unique keys) and c3 (the 5-relation chain), each with
-    device-resident inputs, 100 timed steps, its phase times and the probe
-    roofline.  `--workload c1|c3` runs either with every leg (e2e, CPU
-    baseline)."""
+    device-resident inputs, 100 timed steps, its phase times, the probe
+    roofline and (unless --no-cpu-baseline) the oracle's restatement of
+    execute() on the same inputs with all host threads, at most 20 s each.
+    `--workload c1|c3` runs either with every leg (e2e too)."""
     import copy
     out = {}
     for name in ("c1", "c3"):
         a = copy.copy(args)
         a.workload, a.scale, a.steps, a.warmup = name, 1.0, 100, 3
-        a.no_e2e, a.no_cpu_baseline = True, True
+        a.no_e2e, a.cpu_budget_s = True, min(args.cpu_budget_s, 20.0)
         r = run_ours(a, d)
         out[name] = {"workload": r["config"]["workload"], "steps": r["steps"], "ms_per_step": r["ms_per_step"],
                      "probe_tuples_per_s": r["value"], "build_tuples_per_s": r["build_tuples_per_s"],
                      "output_rows": r["config"]["output_rows"], "phases_ms": r["phases_ms"],
                      "probe_roofline_frac": r["roofline"]["frac"], "probe_achieved_gbs": r["roofline"]["achieved"],
-                     "algorithmic_bytes": r["roofline"]["algorithmic_bytes"], "gpu_launches": r["gpu_launches"]}
+                     "algorithmic_bytes": r["roofline"]["algorithmic_bytes"], "gpu_launches": r["gpu_launches"],
+                     "cpu_baseline": r["cpu_baseline"]}
     return out
 
 
