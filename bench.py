@@ -480,18 +480,20 @@ def run_ours(args, d: Dist) -> dict:
     # ---- phase times from a second pass with per-phase CUDA events (which
     # add about 35 us of host work per execute, so they stay out of `value`)
     eng.set_option("timing", 1)
+    # (per phase the median over the steps: one step that the host stalls
+    # between two events must not move a phase's figure)
     phase_steps = min(args.steps, 50)
-    phase_sum = {}
+    phase_seen = {}
     for _ in range(phase_steps):
         r = eng.execute_raw(resident)
         for k, v in eng.stats(r)[3].items():
-            phase_sum[k] = phase_sum.get(k, 0.0) + v
+            phase_seen.setdefault(k, []).append(v)
         last = r
         if _ < phase_steps - 1:
             eng.free_result(r)
     last_counters = eng.counters(last)
     eng.free_result(last)
-    phases = {k: round(v / phase_steps, 4) for k, v in phase_sum.items() if k != "launches"}
+    phases = {k: round(statistics.median(v), 4) for k, v in phase_seen.items() if k != "launches"}
 
     # ---- roofline of the probe phase: directory words and table tuples of
     # the tables this execute built (summed over its joins)
@@ -531,7 +533,7 @@ def run_ours(args, d: Dist) -> dict:
         "data": "synthetic (seeded generator with the configured shapes; inputs > L2, no flush needed)",
         "config": workload_config(w, args, d.world, nb, npr, nout),
         "build_tuples_per_s": nb * d.world / (ms / 1e3),
-        "phases_ms": phases, "phases_from": f"{phase_steps} further steps with per-phase CUDA events",
+        "phases_ms": phases, "phases_from": f"median of {phase_steps} further steps with per-phase CUDA events",
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
         "gpu_launches": launches, "clocks": clocks,
     }
