@@ -19,8 +19,9 @@ build, probe, and the output written as reference-format pages.
          most about 30 s of CPU time, else a stated probe-side prefix)
 
 The default c2 line also carries `workloads` (c1 and c3 at full size, device
-time and probe roofline of each) and `systems` (the batched and served forms
-at reduced size, each against the plain path).
+time, probe roofline and CPU baseline of each) and `systems` (the batched and
+served forms at reduced size, each against the plain path).  `--workload c4`
+adds a CPU baseline on a seeded 64-instance sample.
 
 The inputs (>2 GB of pages) exceed the 126 MB L2, so no flush is needed
 between steps.  `--impl reference` times the CPU restatement alone, one
