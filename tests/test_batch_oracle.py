@@ -136,3 +136,21 @@ def test_serving_schedule_is_a_seeded_poisson_mix(hj):
     for k, f in zip(serve.KINDS, mix.fractions):
         assert abs((kinds == k).mean() - f) < 0.015
     assert {x[2] for x in a if x[1] == "small"} == set(range(16))
+
+
+def test_bench_c4_cpu_sample(hj, orc):
+    """bench.py's c4 CPU baseline: every sampled instance runs as its left-deep
+    plan through the restated execute(), and its row count is checked against
+    the given (GPU) counts."""
+    import importlib.util
+    from pathlib import Path
+    from hjgb300 import workloads
+    spec = importlib.util.spec_from_file_location("bench", Path(__file__).resolve().parents[1] / "bench.py")
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    w = workloads.c4(n=24, scale=0.004)
+    rows = np.array([bo.chain_result(bo.instance_relations(w.seed, *w.instance(i)))[0] for i in range(len(w))])
+    out = bench.c4_cpu_sample(hj, w, rows, 30.0, n=12)
+    assert out["rows_equal_gpu"] and out["kind"] == "port" and out["value"] > 0
+    assert out["sample"].startswith("12 of a seeded 12-instance sample")
+    assert not bench.c4_cpu_sample(hj, w, rows + 1, 30.0, n=12)["rows_equal_gpu"]
