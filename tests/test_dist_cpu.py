@@ -28,7 +28,8 @@ def _rank(rank: int, world: int, port: int, q) -> None:
     d = bench.Dist()
     d.barrier()
     got = d.max(1.5 + rank)           # each rank's step time; the job's is the slowest
-    q.put((rank, d.world, got))
+    low = -d.max(-(1.5 + rank))       # the lowest over ranks (the e2e link probe)
+    q.put((rank, d.world, got, low))
     d.close()
 
 
@@ -43,7 +44,7 @@ def test_barrier_and_max_over_two_gloo_ranks():
     for p in procs:
         p.join(timeout=60)
         assert p.exitcode == 0
-    assert out == [(0, 2, 2.5), (1, 2, 2.5)]
+    assert out == [(0, 2, 2.5, 1.5), (1, 2, 2.5, 1.5)]
 
 
 def test_reference_arm_under_torchrun_prints_one_line_from_rank_0():
