@@ -213,6 +213,52 @@ def test_host_transfer_paths_agree(engine, orc):
         engine.set_option("host_access", saved)
 
 
+def test_probe_side_int32_outputs_and_type_mismatches(engine, orc, hj):
+    """Probe-side INT32 columns with NULLs on pages of irregular row counts as
+    output columns; the same INT32 column output as INT32 and as VARCHAR (all
+    NULL through the matches: NULL strings), and a non-NULL value through the
+    matches in a VARCHAR output (the reference's error)."""
+    I, V = cases.I, cases.V
+    r = np.random.default_rng(23)
+    n = 100_000
+    keys = r.integers(0, 20_000, n)
+    pay = [None if x else int(v) for x, v in zip(r.random(n) < 0.3, r.integers(-2**31, 2**31 - 1, n))]
+    pay2 = [None if x else int(v) for x, v in zip(r.random(n) < 0.05, r.integers(-5, 5, n))]
+    build = cases.table(hj, [[k, f"s{k}"] for k in range(0, 20_000, 3)], [I, V])
+    probe = cases.table(hj, [[int(k), a, b] for k, a, b in zip(keys, pay, pay2)], [I, I, I])
+    p = hj.Plan()
+    p.new_input(build)
+    p.new_input(probe)
+    p.new_scan_node(0, [(0, I), (1, V)])
+    p.new_scan_node(1, [(0, I), (1, I), (2, I)])
+    p.root = p.new_join_node(True, 0, 1, 0, 0, [(3, I), (0, I), (4, I), (1, V)])
+    assert_same(orc, engine.execute(p), orc.run(orc.port(), p), "probe-side INT32 outputs")
+    # the same INT32 column as INT32 and as VARCHAR output, all NULL through the matches
+    b = cases.table(hj, [[1, "x"], [2, "y"], [5, "z"]], [I, V])
+    pr = cases.table(hj, [[1, None], [2, None], [3, 7], [4, 8], [1, None], [5, None], [9, 11]], [I, I])
+    p = hj.Plan()
+    p.new_input(b)
+    p.new_input(pr)
+    p.new_scan_node(0, [(0, I), (1, V)])
+    p.new_scan_node(1, [(0, I), (1, I)])
+    p.root = p.new_join_node(True, 0, 1, 0, 0, [(3, I), (3, V), (1, V), (2, I)])
+    want = orc.run(orc.port(), p)
+    assert want.status == 0
+    assert_same(orc, engine.execute(p), want, "INT32 column as VARCHAR output")
+    # a non-NULL value through the matches: the reference's error
+    pr = cases.table(hj, [[1, None], [2, 6], [5, None]], [I, I])
+    p = hj.Plan()
+    p.new_input(b)
+    p.new_input(pr)
+    p.new_scan_node(0, [(0, I), (1, V)])
+    p.new_scan_node(1, [(0, I), (1, I)])
+    p.root = p.new_join_node(True, 0, 1, 0, 0, [(3, I), (3, V)])
+    assert orc.run(orc.port(), p).status != 0
+    with pytest.raises(hj.HjError) as e:
+        engine.execute(p)
+    assert e.value.status == hj.HJ_ERR_RUNTIME and "not string or null" in str(e.value)
+
+
 def test_error_classes(engine, hj):
     p = hj.Plan()
     t = cases.table(hj, [["a"], ["b"]], [cases.V])
