@@ -199,7 +199,6 @@ public:
         cv_.notify_all();
         for (auto& w : workers_) w.join();
     }
-    unsigned size() const { return unsigned(workers_.size()); }
 
     // Runs fn(i) for i in [0, n) on the pool and the calling thread.
     void parallel_for(size_t n, const std::function<void(size_t)>& fn) {
